@@ -1,0 +1,431 @@
+"""Benchmark: pair-interactions/s of the all-pairs force + integrate step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (a "step" is one force + integrate iteration over the whole system):
+N = 1,048,576 particles from a seeded Plummer sphere (scale radius 1, total mass
+1), eps2 = 1e-4, dt = 1e-4, damping 1, FP32.  The inputs are generated on the
+host by the library's seeded generator (no dataset).
+
+Prints one JSON line.  `value` is device time with the state resident in HBM
+(CUDA events on the simulation's stream, L2 flushed between timed steps);
+`e2e` is the same metric through the C ABI with host buffers: every step copies
+the state in from pinned host memory, advances, and copies it back.  The CPU
+baseline times the oracle (the reference kernel body restated in C, OpenMP) on
+a bounded sample of i-rows against all N j-particles.  Extra keys report the
+ensemble and adjoint speed-ups of the metric's other two parts.
+
+With --impl reference the line reports the reference's CPU path (the oracle
+port on all host threads) on the same workload, and -- as an extra key -- the
+reference's own CUDA kernel built from its source for sm_103a.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "cuda-to-sycl-nbody_gb300"))
+
+METRIC = "pair-interactions/s & %FP32 peak at N=1M; ensemble+adjoint speedup vs plain"
+UNIT = "pair-interactions/s"
+N_BENCH = 1 << 20
+EPS2 = 1e-4
+DT = 1e-4
+SEED = 20261203
+FLOP_PER_PAIR = 20
+
+
+def workload_desc(n=N_BENCH):
+    return {"workload": f"Plummer sphere N={n}, eps2={EPS2:g}, dt={DT:g}, FP32, one force+integrate "
+                        "iteration per step", "N": n, "eps2": EPS2, "dt": DT, "seed": SEED,
+            "pairs_per_step": n * n, "l2": "flushed between timed steps (512 MiB write)"}
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [s.strip() for s in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- helpers
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if os.environ.get("NB_BENCH_BACKEND") != "gloo" else "gloo")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v: float, world: int) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return json.loads(p.read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_sample_rate(pos, mass_G, target_s: float, max_rows: int | None = None):
+    """Oracle (FP32 restatement, OpenMP) on strided i-rows against all N j.
+    Returns (pairs/s, rows, seconds, threads)."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_binding as orc
+
+    n = pos[0].size
+    rows = 64
+    while True:
+        idx = np.linspace(0, n - 1, rows).astype(np.int64)
+        t0 = time.perf_counter()
+        orc.accel_fp32(pos, None, mass_G, EPS2, rows=idx)
+        dt = time.perf_counter() - t0
+        if dt >= target_s or (max_rows and rows >= max_rows):
+            return rows * n / dt, rows, dt, orc.num_threads()
+        grow = max(2.0, min(8.0, target_s / max(dt, 1e-3)))
+        rows = int(rows * grow)
+        if max_rows:
+            rows = min(rows, max_rows)
+
+
+def plummer_inputs(n=N_BENCH):
+    import nbody_gb300 as nb
+
+    (x, y, z), (vx, vy, vz), m = nb.plummer(SEED, n)
+    return [x, y, z], [vx, vy, vz], m
+
+
+# --------------------------------------------------------------------------- our arm
+def run_ours(args, rank, world) -> dict:
+    import torch
+
+    import nbody_gb300 as nb
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    n = N_BENCH
+    pos, vel, m = plummer_inputs(n)
+    p = nb.SimParam(numParticles=n, G=1.0, dt=DT, damping=1.0, distEps=EPS2)
+    sim = nb.Simulation(p, pos, vel, m)
+    stream = torch.cuda.current_stream()
+    sim.set_stream(stream.cuda_stream)
+    if args.autotune:
+        sim.autotune()
+    kinfo = sim.kernel_info()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    for _ in range(args.warmup):
+        sim.advance(1)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        w0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record(stream)
+            sim.advance(1)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+    sim.synchronize()
+    barrier(world)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    dev_s = max_over_ranks(sum(step_ms) / 1e3, world)
+    pairs = float(n) * n * args.steps * world
+    value = pairs / dev_s
+    ms_per_step = dev_s * 1e3 / args.steps
+
+    # roofline of the force kernel (one launch per step)
+    peak_tf = nb.fp32_peak_tflops()
+    achieved_tf = FLOP_PER_PAIR * float(n) * n / (min(step_ms) * 1e-3) / 1e12
+    roofline = {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
+                "frac": achieved_tf / peak_tf, "traffic": traffic_from_profile(),
+                "peak_source": "nominal: SMs x 128 FP32 lanes x 2 flop x max SM clock "
+                               "(no FP32 peak in MEASURED_PEAKS.json)",
+                "flop_per_pair": FLOP_PER_PAIR,
+                "kernel_ms": {"min": min(step_ms), "median": statistics.median(step_ms)}}
+
+    # e2e through the C ABI with pinned host buffers
+    host = [torch.empty(n, dtype=torch.float32, pin_memory=True).numpy() for _ in range(6)]
+    for h, src in zip(host, pos + vel):
+        h[:] = src
+    e2e_steps = max(1, min(args.steps, 5))
+    sim.set_state(host[:3], host[3:])
+    sim.advance(1)
+    sim.get_state(host)
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.set_state(host[:3], host[3:])   # 6 x N floats host -> device
+        sim.advance(1)
+        sim.get_state(host)                 # 6 x N floats device -> host (synchronizes)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = {"value": float(n) * n * e2e_steps * world / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": 6 * 4 * n, "d2h_bytes_per_step": 6 * 4 * n,
+           "ms_per_step": e2e_s * 1e3 / e2e_steps}
+
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Plummer sphere generated by the library)",
+        "config": dict(workload_desc(n), kernel=kinfo,
+                       parallelism="replicas" if world > 1 else "single GPU"),
+        "gflops": value * FLOP_PER_PAIR / 1e9,
+        "fp32_peak_frac": value * FLOP_PER_PAIR / world / (peak_tf * 1e12),
+        "roofline": roofline, "e2e": e2e, "gpu_launches": args.steps,
+        "clocks": clk.summary(), "wall_s_timed_region": wall,
+    }
+    sim.close()
+    del flush
+    if rank == 0 and not args.no_extras:
+        result["ensemble"] = bench_ensemble(args)
+        result["adjoint"] = bench_adjoint(args)
+    if rank == 0 and not args.no_cpu:
+        rate, rows, secs, thr = cpu_sample_rate(pos, float(np.float32(m[0])), args.cpu_seconds)
+        result["cpu_baseline"] = {
+            "value": rate, "unit": UNIT, "cores": thr, "kind": "port",
+            "sample": f"{rows} strided i-rows x all {n} j-particles of the same workload "
+                      f"({secs:.1f} s), oracle/nbody_oracle.c (FP32 restatement of "
+                      "src/simulator.cu:186-229), OpenMP"}
+    return result
+
+
+def traffic_from_profile():
+    """DRAM bytes per launch of the force kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "force_kernel_plummer_1M.txt"
+    try:
+        for line in f.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch_full_size:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def bench_ensemble(args) -> dict:
+    """Config 3: 4,096 Plummer systems, sizes log-uniform in [64, 8192]."""
+    import torch
+
+    import nbody_gb300 as nb
+
+    sizes = nb.ensemble_sizes(SEED, 4096, 64, 8192)
+    parts = [nb.plummer(SEED + 1 + k, int(s)) for k, s in enumerate(sizes)]
+    pos = [np.concatenate([q[0][c] for q in parts]) for c in range(3)]
+    vel = [np.concatenate([q[1][c] for q in parts]) for c in range(3)]
+    m = np.concatenate([q[2] for q in parts])
+    p = nb.SimParam(G=1.0, dt=1e-3, damping=1.0, distEps=1e-3)
+    sim = nb.Simulation(p, pos, vel, m, sizes=sizes)
+    chosen = sim.autotune()
+    pairs = float(np.sum(sizes.astype(np.float64) ** 2))
+    sim.advance(2)
+    persistent_ms = sim.time_iterations(10) / 10
+    sim.graph_capture(100)
+    sim.graph_launch()
+    sim.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    w = time.perf_counter()
+    sim.graph_launch()
+    sim.synchronize()
+    graph_ms = (time.perf_counter() - w) * 1e3 / 100
+    del t0, t1
+    sim.advance_per_system(1)
+    per_sys_ms = sim.time_iterations(3, per_system=True) / 3
+    info = sim.kernel_info()
+    sim.close()
+    return {"systems": int(len(sizes)), "particles": int(sizes.sum()), "pairs_per_step": pairs,
+            "persistent_ms_per_step": persistent_ms, "graph_ms_per_step": graph_ms,
+            "per_system_launch_ms_per_step": per_sys_ms,
+            "speedup_vs_per_system_launches": per_sys_ms / graph_ms,
+            "pair_interactions_per_s": pairs / (graph_ms * 1e-3), "autotuned_config": chosen,
+            "kernel": info}
+
+
+def bench_adjoint(args) -> dict:
+    """Config 4: N = 16,384 disk, T = 256 iterations, checkpoints every 16."""
+    import nbody_gb300 as nb
+
+    n, T, every = 16384, 256, 16
+    (x, y, z), (vx, vy, vz), m = nb.thin_disk(SEED, n, 1e-3)
+    p = nb.SimParam(numParticles=n, G=1.0, dt=1e-3, damping=0.999, distEps=1e-3)
+    sim = nb.Simulation(p, (x, y, z), (vx, vy, vz), m)
+    sim.advance(2)
+    fwd_ms = sim.time_iterations(T) / T
+    sim.set_state((x, y, z), (vx, vy, vz))
+    gx = np.ones(3 * n, dtype=np.float32) / n
+    sim.adjoint_forward(T, every)
+    sim.adjoint_backward(gx)               # warm-up (allocations)
+    w = time.perf_counter()
+    sim.adjoint_backward(gx)
+    bwd_s = time.perf_counter() - w
+    sim.close()
+    per_step = bwd_s * 1e3 / T
+    return {"N": n, "T": T, "checkpoint_every": every, "forward_ms_per_step": fwd_ms,
+            "backward_ms_per_step": per_step,
+            "adjoint_step_cost_vs_forward": per_step / fwd_ms,
+            "note": "backward = recompute from checkpoints + VJP kernel, per step"}
+
+
+# --------------------------------------------------------------------------- reference arm
+def run_reference(args, rank, world) -> dict | None:
+    if rank != 0:
+        return None
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_binding as orc
+
+    n = N_BENCH
+    pos, vel, m = plummer_inputs(n)
+    G = float(np.float32(m[0]))
+    # size each step to ~ cpu_seconds / (steps + warmup) of work
+    per_step_s = max(1.0, args.cpu_seconds * 2 / max(1, args.steps + args.warmup))
+    rate0, rows, _, thr = cpu_sample_rate(pos, G, per_step_s)
+    idx = np.linspace(0, n - 1, rows).astype(np.int64)
+    for _ in range(args.warmup):
+        orc.accel_fp32(pos, None, G, EPS2, rows=idx)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        orc.accel_fp32(pos, None, G, EPS2, rows=idx)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = rows * n * args.steps / total
+    sample = (f"{rows} strided i-rows x all {n} j-particles per step, oracle/nbody_oracle.c "
+              "(the reference kernel body src/simulator.cu:186-229 restated in C; the reference "
+              "ships no CPU path and its SYCL twin needs a DPC++ toolchain absent here), OpenMP")
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": total * 1e3 / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded Plummer sphere generated by the library)",
+           "config": workload_desc(n),
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": thr, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    if orc.reference_available() and not args.no_extras:
+        try:
+            zeros = [np.zeros(n, np.float32)] * 3
+            orc.reference_run(pos, zeros, G, DT, 1.0, EPS2, 1, gw_size=128)  # warm-up
+            _, ms = orc.reference_run(pos, zeros, G, DT, 1.0, EPS2, 1, gw_size=128)
+            out["reference_cuda_kernel"] = {
+                "value": float(n) * n / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+                "source": "src/simulator.cu particle_interaction<BRANCH> compiled unmodified "
+                          "for sm_103a with -use_fast_math, gwSize 128, CUDA events"}
+        except Exception as e:  # reported, not fatal
+            out["reference_cuda_kernel"] = {"unavailable": str(e).splitlines()[0]}
+    return out
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser(description="GB300 n-body benchmark")
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)  # at least 3 untimed warm-up steps
+    rank, world = dist_init()
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+    else:
+        res = run_ours(args, rank, world)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,78 @@
+// Host-callable launchers of the device kernels (implemented in the .cu files).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "nb_internal.hpp"
+
+namespace nbg {
+
+// ---- force + integrate (force_kernel.cu) ----------------------------------------
+int num_force_configs();
+KernelShape force_config_shape(int index);
+// Launch the tuned force kernel of shape `index`.  `compensated` selects the Kahan
+// accumulator, `per_pair_mass` multiplies each pair term by m_j.
+cudaError_t launch_force(int index, bool compensated, bool per_pair_mass, const ForceArgs& a,
+                         int grid, cudaStream_t stream);
+cudaError_t force_blocks_per_sm(int index, bool compensated, bool per_pair_mass, int* blocks);
+
+// ---- compatibility kernel (aux_kernels.cu) ------------------------------------------
+// The reference's PREDICATED variant as shipped, one thread per i-particle over one
+// system (simulator.cu:186-229 with the (i == id) mask of :208-209).
+cudaError_t launch_predicated(const ForceArgs& a, const SystemDesc& sd, int32_t sys_index,
+                              cudaStream_t stream);
+
+// ---- state movement (aux_kernels.cu) ------------------------------------------------
+// Device SoA staging <-> simulation layout.  `map` holds, for each of the n real
+// particles in user order, its padded device index.
+cudaError_t launch_unpack_state(const float* soa /*[7][n]: x y z vx vy vz m*/, int64_t n,
+                                const int64_t* map, float* pos, float4* vel, bool with_mass,
+                                cudaStream_t stream);
+cudaError_t launch_pack_state(const float* pos, const float4* vel, int64_t n, const int64_t* map,
+                              float* soa /*[6][n]*/, cudaStream_t stream);
+cudaError_t launch_pack_accel(const float4* acc, int64_t n, const int64_t* map,
+                              float* soa /*[3][n]*/, cudaStream_t stream);
+cudaError_t launch_export(const float* pos, const float4* vel, int64_t n, const int64_t* map,
+                          float4* pos_out, float4* vel_out, cudaStream_t stream);
+cudaError_t launch_fill_padding(float* pos, float4* vel, int64_t n_pad_total, cudaStream_t stream);
+
+// ---- FP64 diagnostics (diag_kernels.cu) ---------------------------------------------
+struct DiagScratch {
+  double* partial;   // [max_blocks][10]
+  int32_t max_blocks;
+};
+cudaError_t launch_diagnostics(const float* pos, const float4* vel, const SystemDesc* sys_d,
+                               const SystemDesc* sys_h, int32_t first_sys, int32_t num_sys,
+                               float eps2, float G, bool per_pair_mass, double* out10,
+                               DiagScratch& scratch, cudaStream_t stream);
+cudaError_t launch_fp64_rows(const float* pos, const SystemDesc* sys_d, const int64_t* rows_dev,
+                             const int32_t* row_sys_dev, int64_t count, float eps2, float G,
+                             bool per_pair_mass, double* out3, cudaStream_t stream);
+
+// ---- adjoint (adjoint_kernel.cu) ----------------------------------------------------
+struct AdjointArgs {
+  const float* pos;       // pair layout, positions x_t at which the Jacobian is taken
+  const float4* mu;       // [n_pad] adjoint vector mu = lam_v' + dt lam_x' (w unused)
+  const float4* lam_x;    // [n_pad] lam_x'
+  float4* lam_x_out;      // [n_pad] lam_x = lam_x' + dt * G * J^T mu
+  const SystemDesc* sys;
+  const int32_t* tile_sys;  // [tiles] system of each i-tile
+  const int32_t* tile_idx;  // [tiles] i-tile index within its system
+  float eps2;
+  float dt;
+  int32_t mask_self;
+};
+cudaError_t launch_adjoint(const AdjointArgs& a, int32_t num_tiles, bool per_pair_mass,
+                           cudaStream_t stream);
+int adjoint_tile();  // i-particles per adjoint CTA
+cudaError_t launch_adjoint_prepare(const float4* lam_x, const float4* lam_v, float4* mu,
+                                   float dt, int64_t n_pad, cudaStream_t stream);
+cudaError_t launch_adjoint_finish_v(const float4* mu, float4* lam_v_out, float damping,
+                                    int64_t n_pad, cudaStream_t stream);
+// n x 3 interleaved (user order) <-> padded float4.
+cudaError_t launch_unpack_vec3(const float* in, int64_t n, const int64_t* map, float4* out,
+                               cudaStream_t stream);
+cudaError_t launch_pack_vec3(const float4* in, int64_t n, const int64_t* map, float* out,
+                             cudaStream_t stream);
+
+}  // namespace nbg

@@ -1,0 +1,146 @@
+// The simulation object behind the opaque nb_sim handle, and runtime helpers
+// shared by the host translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "nb_internal.hpp"
+#include "nb_kernels.hpp"
+#include "nbody_gb300.h"
+
+namespace nbg {
+
+struct WorkListDev {
+  int32_t cfg = -1;
+  int32_t grid = 0;
+  int32_t nseg = 0;
+  int32_t nfix = 0;
+  int32_t slots = 0;
+  int32_t split = 0;
+  Segment* segs = nullptr;
+  int32_t* seg_begin = nullptr;
+  Fixup* fix = nullptr;
+};
+
+// Checkpoints and work buffers of the adjoint (allocated on first use).
+struct AdjointState {
+  int32_t T = 0;
+  int32_t every = 0;
+  int32_t count = 0;                // number of checkpoints stored
+  int32_t start_cur = 0;
+  std::vector<float*> ckpt_pos;     // pair layout, n_pad * 4 floats each
+  std::vector<float4*> ckpt_vel;
+  std::vector<float*> seg_pos;      // positions of one recomputed segment
+  float4* lam_x = nullptr;
+  float4* lam_v = nullptr;
+  float4* mu = nullptr;
+  float4* tmp = nullptr;
+  float4* vel = nullptr;            // velocities of the recomputed segment
+  int32_t* tile_sys = nullptr;
+  int32_t* tile_idx = nullptr;
+  int32_t num_tiles = 0;
+  bool valid = false;
+};
+
+}  // namespace nbg
+
+struct nb_sim {
+  nb_params params{};
+  int sms = 0;
+  std::string device_name;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+
+  std::vector<nbg::SystemDesc> sys_h;
+  std::vector<int64_t> user_offset;  // first user index of each system
+  uint64_t n_real = 0;
+  int64_t n_pad = 0;
+  nbg::SystemDesc* sys_d = nullptr;
+  int64_t* map_d = nullptr;  // user index -> padded index (NULL: identity, one system)
+
+  float* pos_d[2] = {nullptr, nullptr};  // pair layout, double-buffered
+  int cur = 0;
+  float4* vel_d = nullptr;
+  float4* acc_d = nullptr;
+  float* staging_d = nullptr;  // [7][n_real]
+  int32_t* err_d = nullptr;
+  bool per_pair_mass = false;
+  int32_t mask_self = 0;
+
+  int cfg = 0;
+  nbg::WorkListDev wl;
+  std::vector<nbg::WorkListDev> wl_sys;
+  int wl_sys_cfg = -1;
+  float4* partials_d = nullptr;
+  size_t partials_cap = 0;
+  int32_t* counters_d = nullptr;
+  size_t counters_cap = 0;
+
+  cudaEvent_t ev0 = nullptr;
+  cudaEvent_t ev1 = nullptr;
+  float last_ms = 0.f;
+
+  cudaGraph_t graph[2] = {nullptr, nullptr};        // indexed by starting buffer
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  int32_t graph_iters = 0;
+
+  nbg::DiagScratch diag{};
+  double* diag_out_d = nullptr;
+  nbg::AdjointState adj;
+};
+
+namespace nbg {
+
+extern thread_local std::string t_last_error;
+int set_error(int code, const std::string& msg);
+int cuda_error(cudaError_t e, const char* what);
+int check_device(int* sms, cudaDeviceProp* prop);
+void free_worklist(WorkListDev& w);
+// Free the diagnostics and adjoint buffers of a simulation.
+void release_aux(nb_sim* s);
+
+template <class T>
+int dev_alloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return NB_OK;
+  const cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return cuda_error(e, "cudaMalloc");
+  }
+  return NB_OK;
+}
+
+template <class T>
+void dev_free(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+// Shared by the host translation units (nbody_capi.cpp).
+ForceArgs base_args(nb_sim* s);
+// One force evaluation over all systems: integrate into the other position
+// buffer and swap (accel_out == nullptr), or write accelerations.
+int force_pass(nb_sim* s, float4* accel_out, bool per_system);
+int check_error_word(nb_sim* s);
+int ensure_staging(nb_sim* s);
+int ensure_accel(nb_sim* s);
+// Launch the force kernel with arguments `a` over work list `w`.
+int launch_with(nb_sim* s, ForceArgs a, const WorkListDev& w);
+
+#define NB_TRY(expr)            \
+  do {                          \
+    const int s_ = (expr);      \
+    if (s_ != NB_OK) return s_; \
+  } while (0)
+#define NB_CUDA(expr)                                          \
+  do {                                                         \
+    const cudaError_t e_ = (expr);                             \
+    if (e_ != cudaSuccess) return ::nbg::cuda_error(e_, #expr); \
+  } while (0)
+
+}  // namespace nbg
