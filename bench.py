@@ -182,7 +182,7 @@ def run_ours(args, rank, world) -> dict:
     import nbody_gb300 as nb
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    n = N_BENCH
+    n = args.n
     pos, vel, m = plummer_inputs(n)
     p = nb.SimParam(numParticles=n, G=1.0, dt=DT, damping=1.0, distEps=EPS2)
     sim = nb.Simulation(p, pos, vel, m)
@@ -191,7 +191,7 @@ def run_ours(args, rank, world) -> dict:
     if args.autotune:
         sim.autotune()
     kinfo = sim.kernel_info()
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(max(1, args.flush_mib) << 20, dtype=torch.uint8, device="cuda")
 
     for _ in range(args.warmup):
         sim.advance(1)
@@ -203,7 +203,8 @@ def run_ours(args, rank, world) -> dict:
     with ClockSampler(torch.cuda.current_device()) as clk:
         w0 = time.perf_counter()
         for k in range(args.steps):
-            flush.zero_()
+            if args.flush_mib:
+                flush.zero_()
             starts[k].record(stream)
             sim.advance(1)
             ends[k].record(stream)
@@ -252,7 +253,9 @@ def run_ours(args, rank, world) -> dict:
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Plummer sphere generated by the library)",
-        "config": dict(workload_desc(n), kernel=kinfo,
+        "config": dict(workload_desc(n), kernel=kinfo, l2=(
+                           f"flushed between timed steps ({args.flush_mib} MiB write)"
+                           if args.flush_mib else "not flushed (profiling run)"),
                        parallelism="replicas" if world > 1 else "single GPU"),
         "gflops": value * FLOP_PER_PAIR / 1e9,
         "fp32_peak_frac": value * FLOP_PER_PAIR / world / (peak_tf * 1e12),
@@ -358,7 +361,7 @@ def run_reference(args, rank, world) -> dict | None:
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_binding as orc
 
-    n = N_BENCH
+    n = args.n
     pos, vel, m = plummer_inputs(n)
     G = float(np.float32(m[0]))
     # size each step to ~ cpu_seconds / (steps + warmup) of work
@@ -408,7 +411,12 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--n", type=int, default=N_BENCH,
+                    help="particles (default: the 1,048,576-particle workload; smaller values "
+                         "are for profiling only)")
     ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--flush-mib", type=int, default=512,
+                    help="L2 flush buffer written between timed steps (0: no flush; profiling)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
     args = ap.parse_args()

@@ -203,10 +203,14 @@ __global__ void __launch_bounds__(THREADS) force_kernel(const ForceArgs a) {
     const int count = min(BJ, sd.npad - p_jt * BJ);
     const int64_t first = sd.offset + static_cast<int64_t>(p_jt) * BJ;
     const uint32_t slot = issued % STAGES;
-    fence_proxy_async_smem();
-    mbar_arrive_expect_tx(&full_bar[slot], static_cast<uint32_t>(count) * 16u);
-    bulk_g2s(smem + slot * TILE_BYTES, a.pos + first * 4, static_cast<uint32_t>(count) * 16u,
-             &full_bar[slot]);
+    // Failure-detection test: leave the first tile's barrier without arrival or
+    // copy, so the consumers' bounded wait on it runs out.
+    if (!(a.skip_first_tile && issued == 0)) {
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&full_bar[slot], static_cast<uint32_t>(count) * 16u);
+      bulk_g2s(smem + slot * TILE_BYTES, a.pos + first * 4, static_cast<uint32_t>(count) * 16u,
+               &full_bar[slot]);
+    }
     ++issued;
     if (++p_jt >= sg.jt1) {
       ++p_seg;

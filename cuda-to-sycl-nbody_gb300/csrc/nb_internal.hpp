@@ -76,6 +76,7 @@ struct ForceArgs {
   float dt;
   float damping;
   int32_t mask_self;        // 1: exclude j == i explicitly (eps2^3 underflows)
+  int32_t skip_first_tile;  // failure-detection test: never copy each CTA's first j-tile
 };
 
 // Host description of one kernel shape.

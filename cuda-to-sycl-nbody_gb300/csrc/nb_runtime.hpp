@@ -70,6 +70,7 @@ struct nb_sim {
   int32_t* err_d = nullptr;
   bool per_pair_mass = false;
   int32_t mask_self = 0;
+  int32_t inject_timeout = 0;  // one-shot failure-detection switch
 
   int cfg = 0;
   nbg::WorkListDev wl;

@@ -246,10 +246,13 @@ ForceArgs base_args(nb_sim* s) {
   a.dt = s->params.dt;
   a.damping = s->params.damping;
   a.mask_self = s->mask_self;
+  a.skip_first_tile = 0;
   return a;
 }
 
 int launch_with(nb_sim* s, ForceArgs a, const WorkListDev& w) {
+  a.skip_first_tile = s->inject_timeout;
+  s->inject_timeout = 0;
   a.segs = w.segs;
   a.seg_begin = w.seg_begin;
   a.fix = w.fix;
@@ -281,7 +284,11 @@ int check_error_word(nb_sim* s) {
   NB_CUDA(cudaMemcpyAsync(&err, s->err_d, sizeof(err), cudaMemcpyDeviceToHost, s->stream));
   NB_CUDA(cudaStreamSynchronize(s->stream));
   if (err != 0) {
+    // CTAs that gave up never arrived on their fixup counters: clear them.
     NB_CUDA(cudaMemsetAsync(s->err_d, 0, sizeof(int32_t), s->stream));
+    if (s->counters_d)
+      NB_CUDA(cudaMemsetAsync(s->counters_d, 0, s->counters_cap * sizeof(int32_t), s->stream));
+    NB_CUDA(cudaStreamSynchronize(s->stream));
     return set_error(NB_ERR_DEVICE_TIMEOUT,
                      "a bounded device-side wait timed out (error word " + std::to_string(err) +
                          "); results of that launch are invalid");
@@ -781,6 +788,14 @@ int nb_plan_work(uint32_t num_systems, const uint32_t* sizes, int32_t config_ind
     std::memcpy(segments, h.segs.data(), h.segs.size() * sizeof(Segment));
   }
   if (seg_begin) std::memcpy(seg_begin, h.seg_begin.data(), h.seg_begin.size() * sizeof(int32_t));
+  return NB_OK;
+}
+
+int nb_sim_inject_wait_timeout(nb_sim* s) {
+  if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  if (s->params.calc_method != NB_BRANCH)
+    return set_error(NB_ERR_STATE, "the PREDICATED kernel has no device-side waits");
+  s->inject_timeout = 1;
   return NB_OK;
 }
 

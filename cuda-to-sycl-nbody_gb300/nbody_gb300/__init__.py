@@ -100,6 +100,7 @@ SIGNATURES = {
     "nb_sim_advance": (C.c_int, [_P, C.c_int32]),
     "nb_sim_advance_per_system": (C.c_int, [_P, C.c_int32]),
     "nb_sim_synchronize": (C.c_int, [_P]),
+    "nb_sim_inject_wait_timeout": (C.c_int, [_P]),
     "nb_sim_time_iterations": (C.c_int, [_P, C.c_int32, C.c_int32, _F]),
     "nb_sim_get_state": (C.c_int, [_P] + [_F] * 6),
     "nb_sim_set_state": (C.c_int, [_P] + [_F] * 7),
@@ -343,6 +344,10 @@ class Simulation:
 
     def synchronize(self) -> None:
         _check(lib.nb_sim_synchronize(self._h))
+
+    def inject_wait_timeout(self) -> None:
+        """Failure-detection test hook: the next launch's bounded waits run out."""
+        _check(lib.nb_sim_inject_wait_timeout(self._h))
 
     def time_iterations(self, iterations: int, per_system: bool = False) -> float:
         ms = C.c_float()

@@ -152,6 +152,12 @@ int nb_sim_step(nb_sim* s);
 int nb_sim_advance(nb_sim* s, int32_t iterations);
 /* Baseline for ensembles: the same iterations issued as one launch per system. */
 int nb_sim_advance_per_system(nb_sim* s, int32_t iterations);
+/* Failure-detection test hook (one shot): the next force launch leaves the
+ * first shared-memory tile of every CTA uncopied, so each CTA's bounded wait
+ * (2 s) runs out; the launch writes no results, and the next
+ * nb_sim_synchronize / nb_sim_get_state returns NB_ERR_DEVICE_TIMEOUT.  No
+ * memory is faulted and nothing hangs; the simulation stays usable. */
+int nb_sim_inject_wait_timeout(nb_sim* s);
 /* Wait for the stream and report any device-side error (e.g. a wait that timed out). */
 int nb_sim_synchronize(nb_sim* s);
 /* Run `iterations` iterations bracketed by CUDA events on the simulation's stream

@@ -1,0 +1,76 @@
+"""GPU FP64 diagnostics (energy, momenta, FP64 acceleration rows) against the
+CPU FP64 oracle, and the conservation laws the step must respect."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import nbody_gb300 as nb
+import oracle_binding as orc
+from helpers import disk_case, params
+
+pytestmark = pytest.mark.gpu
+EPS32 = float(np.float32(1e-3))
+
+
+@pytest.mark.parametrize("n", [2, 333, 5000])
+def test_energy_and_momenta_match_fp64_oracle(n):
+    pos, vel, m = disk_case(n, seed=n + 1)
+    with nb.Simulation(params(n), pos, vel, m) as sim:
+        d = sim.diagnostics()
+    ref = orc.energy_fp64(pos, vel, m, 1.0, EPS32)
+    assert np.isclose(d["kinetic"], ref["kinetic"], rtol=1e-12)
+    assert np.isclose(d["potential"], ref["potential"], rtol=1e-11)
+    assert np.isclose(d["mass"], ref["mass"], rtol=1e-12)
+    for a, b in zip(d["momentum"] + d["angular_momentum"],
+                    ref["momentum"] + ref["angular_momentum"]):
+        assert abs(a - b) <= 1e-12 * (1 + abs(b))
+
+
+def test_ensemble_diagnostics_per_system_and_total():
+    sizes = [40, 1000, 17]
+    parts = [disk_case(s, seed=200 + k) for k, s in enumerate(sizes)]
+    pos = [np.concatenate([p[0][c] for p in parts]) for c in range(3)]
+    vel = [np.concatenate([p[1][c] for p in parts]) for c in range(3)]
+    m = np.concatenate([p[2] for p in parts])
+    with nb.Simulation(params(sum(sizes)), pos, vel, m, sizes=sizes) as sim:
+        per = [sim.diagnostics(k) for k in range(len(sizes))]
+        tot = sim.diagnostics(-1)
+    for k, (ps, vs, ms) in enumerate(parts):
+        ref = orc.energy_fp64(ps, vs, ms, 1.0, EPS32)
+        assert np.isclose(per[k]["potential"], ref["potential"], rtol=1e-11)
+        assert np.isclose(per[k]["kinetic"], ref["kinetic"], rtol=1e-12)
+    assert np.isclose(tot["potential"], sum(d["potential"] for d in per), rtol=1e-12)
+    assert np.isclose(tot["kinetic"], sum(d["kinetic"] for d in per), rtol=1e-12)
+
+
+def test_momentum_conserved_without_damping():
+    n = 8192
+    pos, vel, m = disk_case(n, seed=9)
+    with nb.Simulation(params(n, damping=1.0), pos, vel, m) as sim:
+        p0 = np.array(sim.diagnostics()["momentum"])
+        sim.advance(50)
+        p1 = np.array(sim.diagnostics()["momentum"])
+    scale = float(np.sum(m * np.abs(vel[0])))
+    assert np.all(np.abs(p1 - p0) < 1e-5 * scale)
+
+
+def test_energy_drift_small_without_damping():
+    n = 4096
+    pos, vel, m = disk_case(n, seed=10)
+    with nb.Simulation(params(n, damping=1.0, dt=1e-4), pos, vel, m) as sim:
+        e0 = sim.diagnostics()["total"]
+        sim.advance(100)
+        e1 = sim.diagnostics()["total"]
+    assert abs(e1 - e0) < 1e-4 * abs(e0)
+
+
+def test_fp64_rows_match_oracle_rows():
+    n = 3000
+    pos, vel, m = disk_case(n, seed=12)
+    rows = np.array([0, 1, 17, 1499, 2999], dtype=np.uint64)
+    with nb.Simulation(params(n), pos, vel, m) as sim:
+        got = sim.fp64_accelerations(rows)
+    ref = orc.accel_fp64(pos, m, 1.0, EPS32, rows=rows.astype(np.int64))
+    for a, b in zip(got, ref):
+        assert np.allclose(a, b, rtol=1e-12, atol=1e-14)

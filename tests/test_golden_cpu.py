@@ -1,0 +1,54 @@
+"""Pin the CPU oracle to the reference kernel: golden vectors produced by the
+reference's own particle_interaction (src/simulator.cu:186-229, compiled
+unmodified for sm_103a; tests/golden/make_golden.py) against the oracle's FP32
+restatement on the same inputs."""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle_binding as orc
+from helpers import vec_errors
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+CASES = sorted(p.stem for p in GOLDEN.glob("*.npz"))
+
+
+def load(name):
+    d = np.load(GOLDEN / f"{name}.npz")
+    p = json.loads(str(d["params"]))
+    pos = [d["x"], d["y"], d["z"]]
+    vel = [d["vx"], d["vy"], d["vz"]]
+    out = [d[f"out_{c}"] for c in ("x", "y", "z", "vx", "vy", "vz")]
+    return pos, vel, out, p
+
+
+def test_golden_set_present():
+    assert {"config0_n2048", "force_sum_n1000", "perf_args_n1280", "predicated_n512",
+            "ragged_n333", "reference_default_n1024"} <= set(CASES)
+    idx = json.loads((GOLDEN / "index.json").read_text())
+    assert len(idx["cubin_sha256"]) == 64
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_matches_reference_kernel(name):
+    pos, vel, out, p = load(name)
+    got = orc.run_fp32(pos, vel, None, p["G"], p["dt"], p["damping"], p["eps"], p["iters"],
+                       method=p["method"])
+    if p["method"] == orc.PREDICATED:
+        # zero force: v' = v * damping, x' = x + v' dt, the same IEEE operations
+        for g, r in zip(got, out):
+            assert np.array_equal(g, r)
+        return
+    if p["damping"] == 0.0 and p["dt"] == 1.0:
+        # force sums (v' = F): accelerations within 1e-5 relative RMS, 1e-4 max
+        rms, mx = vec_errors(got[3:], out[3:])
+        assert rms <= 1e-5 and mx <= 1e-4
+        return
+    scale = max(float(np.max(np.abs(r))) for r in out[:3])
+    assert max(float(np.max(np.abs(g - r))) for g, r in zip(got[:3], out[:3])) <= 1e-4 * scale
+    vscale = max(float(np.max(np.abs(r))) for r in out[3:])
+    assert max(float(np.max(np.abs(g - r))) for g, r in zip(got[3:], out[3:])) <= 1e-4 * vscale

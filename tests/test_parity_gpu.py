@@ -8,6 +8,9 @@ the oracle):
 """
 from __future__ import annotations
 
+import json
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -16,10 +19,12 @@ import oracle_binding as orc
 from helpers import disk_case, g_eff, params, vec_errors
 
 pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
 
 ACC_RMS = 1e-5
 ACC_MAX = 1e-4
 POS_REL = 1e-4
+EPS32 = float(np.float32(1e-3))  # the softening as the library stores it
 
 
 def make_sim(n, seed=1, eps=1e-3, method=nb.BRANCH, acc=nb.ACC_PLAIN, mass="equal", cfg=None,
@@ -53,7 +58,7 @@ def test_accelerations_match_oracle(n):
         got = sim.accelerations()
     om, G = oracle_G(m)
     ref32 = orc.accel_fp32(pos, om, G, 1e-3)
-    ref64 = orc.accel_fp64(pos, m, 1.0, 1e-3)
+    ref64 = orc.accel_fp64(pos, m, 1.0, EPS32)
     if n == 1:
         assert all(np.all(g == 0) for g in got)
         return
@@ -99,10 +104,10 @@ def test_config0_accelerations_against_fp64():
         got = sim.accelerations()
         rows = np.arange(0, n, 7)
         f64 = sim.fp64_accelerations(rows)
-    ref = orc.accel_fp64(pos, m, 1.0, 1e-3)
+    ref = orc.accel_fp64(pos, m, 1.0, EPS32)
     rms, mx = vec_errors(got, ref)
     assert rms <= ACC_RMS and mx <= ACC_MAX
-    # the GPU FP64 rows agree with the CPU FP64 oracle
+    # the GPU FP64 rows agree with the CPU FP64 oracle (same float32 softening)
     for a, b in zip(f64, ref):
         assert np.allclose(a, b[rows], rtol=1e-10, atol=1e-12)
 
@@ -262,3 +267,27 @@ def test_ten_steps_match_reference_kernel(method):
     if method == nb.PREDICATED:
         for g, r in zip(got, ref):
             assert np.array_equal(g, r)
+
+
+@pytest.mark.parametrize("name", sorted(p.stem for p in GOLDEN.glob("*.npz")))
+def test_library_matches_golden_fixtures(name):
+    d = np.load(GOLDEN / f"{name}.npz")
+    prm = json.loads(str(d["params"]))
+    pos = [d["x"], d["y"], d["z"]]
+    vel = [d["vx"], d["vy"], d["vz"]]
+    out = [d[f"out_{c}"] for c in ("x", "y", "z", "vx", "vy", "vz")]
+    n = pos[0].size
+    p = nb.SimParam(numParticles=n, G=prm["G"], dt=prm["dt"], damping=prm["damping"],
+                    distEps=prm["eps"], calcMethod=prm["method"])
+    with nb.Simulation(p, pos, vel, None) as sim:
+        sim.advance(prm["iters"])
+        got = sim.get_state()
+    if prm["method"] == nb.PREDICATED:
+        for g, r in zip(got, out):
+            assert np.array_equal(g, r)
+    elif prm["damping"] == 0.0 and prm["dt"] == 1.0:
+        rms, mx = vec_errors(got[3:], out[3:])
+        assert rms <= ACC_RMS and mx <= ACC_MAX
+    else:
+        scale = max(float(np.max(np.abs(r))) for r in out[:3])
+        assert max(float(np.max(np.abs(g - r))) for g, r in zip(got[:3], out[:3])) <= POS_REL * scale
