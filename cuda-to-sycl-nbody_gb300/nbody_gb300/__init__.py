@@ -125,6 +125,7 @@ SIGNATURES = {
     "nb_sim_fp64_accelerations": (C.c_int, [_P, _U64, C.c_uint64, _D, _D, _D]),
     "nb_sim_adjoint_forward": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "nb_sim_adjoint_backward": (C.c_int, [_P] + [_F] * 4),
+    "nb_accelerations_noalloc": (C.c_int, [_P, C.c_uint64, C.c_float, C.c_float, _P, _P]),
     "nb_ic_thin_disk": (C.c_int, [C.c_uint64, C.c_uint64, C.c_float] + [_F] * 7),
     "nb_ic_plummer": (C.c_int, [C.c_uint64, C.c_uint64] + [_F] * 7),
     "nb_ic_two_disks": (C.c_int, [C.c_uint64, C.c_uint64, C.c_float] + [_F] * 7),
@@ -236,6 +237,14 @@ def plan_work(sizes, config_index: int, max_grid: int):
     arr = np.ctypeslib.as_array(C.cast(segs, _I32), shape=(max(1, nseg.value) * 6,))
     arr = arr.reshape(-1, 6)[: nseg.value].copy()
     return grid.value, arr, begin, nfix.value, slots.value
+
+
+def accelerations_noalloc(pos_xyzm_ptr: int, n: int, G: float, dist_eps: float,
+                          accel_xyzw_ptr: int, stream_ptr: int | None = None) -> None:
+    """nb_accelerations_noalloc on caller device buffers (float4 per particle)."""
+    _check(lib.nb_accelerations_noalloc(C.c_void_p(pos_xyzm_ptr), n, G, dist_eps,
+                                        C.c_void_p(accel_xyzw_ptr),
+                                        C.c_void_p(stream_ptr) if stream_ptr else None))
 
 
 # ---------------------------------------------------------------------------- initial conditions

@@ -238,6 +238,23 @@ int nb_sim_adjoint_forward(nb_sim* s, int32_t T, int32_t checkpoint_every);
 int nb_sim_adjoint_backward(nb_sim* s, const float* gx_T, const float* gv_T,
                             float* gx_0, float* gv_0);
 
+/* ---- accelerations without allocation ------------------------------------------ */
+/* For callers that cannot allocate GPU memory themselves or through this library
+ * -- an engine or plugin host that hands out all device memory from its own
+ * pools, or a frame loop that must not stall on cudaMalloc.  No counterpart in
+ * the reference.  The caller passes n particles as float4 (x, y, z, mass) in
+ * `pos_xyzm_device` and receives float4 (ax, ay, az, 0) in `accel_xyzw_device`
+ * (both device memory, 16-byte aligned); a = G * sum_{j != i} m_j r_ij /
+ * (|r_ij|^2 + dist_eps)^(3/2).  The call allocates no memory: its scratch is one
+ * fixed 13 MiB device array inside the library, which limits n to 262,144
+ * (larger n: NB_ERR_INVALID_ARGUMENT) and which every GPU that loads the library
+ * keeps until the process exits.  The first call on a device looks that array up
+ * and should come before any stream capture.  All calls share the array:
+ * calls whose work overlaps on the GPU (e.g. on two streams at once) race.  Runs
+ * on `stream` and waits for it before returning. */
+int nb_accelerations_noalloc(const float* pos_xyzm_device, uint64_t n, float G, float dist_eps,
+                             float* accel_xyzw_device, void* stream);
+
 /* ---- initial conditions (host, seeded, deterministic) -------------------------------- */
 /* Thin disk: r = sqrt(u), theta uniform, z ~ N(0, 0.01^2), tangential speed
  * r * sqrt(n m r^2 / (r^2 + eps)^1.5) + N(0, 0.01) per component, m = 1/n. */
