@@ -176,6 +176,36 @@ def plummer_inputs(n=N_BENCH):
 
 
 # --------------------------------------------------------------------------- our arm
+def force_error_vs_fp64(sim, n, rows_count=1024):
+    """FP32 accelerations of the simulation's current state against GPU FP64
+    accelerations on strided rows: (relative RMS, max per-row relative)."""
+    rows = np.linspace(0, n - 1, rows_count).astype(np.uint64)
+    a32 = sim.accelerations()
+    a64 = sim.fp64_accelerations(rows)
+    g = np.stack([a[rows.astype(np.int64)].astype(np.float64) for a in a32])
+    r = np.stack(a64)
+    err = np.linalg.norm(g - r, axis=0)
+    mag = np.linalg.norm(r, axis=0)
+    return (float(np.sqrt(np.mean(err ** 2) / np.mean(mag ** 2))),
+            float(np.max(err / np.maximum(mag, 1e-300))), int(rows_count))
+
+
+def time_steps(sim, stream, flush, steps, flush_mib):
+    """Per-step CUDA-event times (ms) on `stream`, L2 flushed between steps."""
+    import torch
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for k in range(steps):
+        if flush_mib:
+            flush.zero_()
+        starts[k].record(stream)
+        sim.advance(1)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in zip(starts, ends)]
+
+
 def run_ours(args, rank, world) -> dict:
     import torch
 
@@ -184,85 +214,101 @@ def run_ours(args, rank, world) -> dict:
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     n = args.n
     pos, vel, m = plummer_inputs(n)
-    p = nb.SimParam(numParticles=n, G=1.0, dt=DT, damping=1.0, distEps=EPS2)
-    sim = nb.Simulation(p, pos, vel, m)
     stream = torch.cuda.current_stream()
-    sim.set_stream(stream.cuda_stream)
-    if args.autotune:
-        sim.autotune()
-    kinfo = sim.kernel_info()
     flush = torch.empty(max(1, args.flush_mib) << 20, dtype=torch.uint8, device="cuda")
-
-    for _ in range(args.warmup):
-        sim.advance(1)
-    torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    barrier(world)
-    torch.cuda.synchronize()
-    with ClockSampler(torch.cuda.current_device()) as clk:
-        w0 = time.perf_counter()
-        for k in range(args.steps):
-            if args.flush_mib:
-                flush.zero_()
-            starts[k].record(stream)
-            sim.advance(1)
-            ends[k].record(stream)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - w0
-    sim.synchronize()
-    barrier(world)
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    dev_s = max_over_ranks(sum(step_ms) / 1e3, world)
-    pairs = float(n) * n * args.steps * world
-    value = pairs / dev_s
-    ms_per_step = dev_s * 1e3 / args.steps
-
-    # roofline of the force kernel (one launch per step)
     peak_tf = nb.fp32_peak_tflops()
-    achieved_tf = FLOP_PER_PAIR * float(n) * n / (min(step_ms) * 1e-3) / 1e12
-    roofline = {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
-                "frac": achieved_tf / peak_tf, "traffic": traffic_from_profile(),
-                "peak_source": "nominal: SMs x 128 FP32 lanes x 2 flop x max SM clock "
-                               "(no FP32 peak in MEASURED_PEAKS.json)",
-                "flop_per_pair": FLOP_PER_PAIR,
-                "kernel_ms": {"min": min(step_ms), "median": statistics.median(step_ms)}}
 
-    # e2e through the C ABI with pinned host buffers
-    host = [torch.empty(n, dtype=torch.float32, pin_memory=True).numpy() for _ in range(6)]
-    for h, src in zip(host, pos + vel):
-        h[:] = src
-    e2e_steps = max(1, min(args.steps, 5))
-    sim.set_state(host[:3], host[3:])
-    sim.advance(1)
-    sim.get_state(host)
-    torch.cuda.synchronize()
-    barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        sim.set_state(host[:3], host[3:])   # 6 x N floats host -> device
+    # Both accumulators: force error against FP64 at the initial state, then the rate.
+    modes = {}
+    for name, acc in (("plain", nb.ACC_PLAIN), ("compensated", nb.ACC_COMPENSATED)):
+        if args.acc != "auto" and args.acc != name:
+            continue
+        p = nb.SimParam(numParticles=n, G=1.0, dt=DT, damping=1.0, distEps=EPS2, accumulator=acc)
+        sim = nb.Simulation(p, pos, vel, m)
+        sim.set_stream(stream.cuda_stream)
+        if args.autotune:
+            sim.autotune()
+        rms, mx, nrows = force_error_vs_fp64(sim, n) if not args.no_accuracy else (None, None, 0)
+        modes[name] = {"sim": sim, "force_rel_rms_vs_fp64": rms, "force_rel_max_vs_fp64": mx,
+                       "rows": nrows}
+    # Headline mode: plain if it meets the 1e-5 relative-RMS target, else compensated.
+    target = 1e-5
+    head = "plain" if ("plain" in modes and (modes["plain"]["force_rel_rms_vs_fp64"] or 0) <= target) \
+        else ("compensated" if "compensated" in modes else "plain")
+    order = [head] + [k for k in modes if k != head]
+
+    result = None
+    for name in order:
+        sim = modes[name]["sim"]
+        kinfo = sim.kernel_info()
+        for _ in range(args.warmup):
+            sim.advance(1)
+        torch.cuda.synchronize()
+        barrier(world)
+        torch.cuda.synchronize()
+        if name == head:
+            with ClockSampler(torch.cuda.current_device()) as clk:
+                w0 = time.perf_counter()
+                step_ms = time_steps(sim, stream, flush, args.steps, args.flush_mib)
+                wall = time.perf_counter() - w0
+        else:
+            step_ms = time_steps(sim, stream, flush, min(args.steps, 5), args.flush_mib)
+        sim.synchronize()
+        barrier(world)
+        dev_s = max_over_ranks(sum(step_ms) / 1e3, world)
+        rate = float(n) * n * len(step_ms) * world / dev_s
+        modes[name].update({"value": rate, "unit": UNIT, "ms_per_step": dev_s * 1e3 / len(step_ms),
+                            "fp32_peak_frac": rate * FLOP_PER_PAIR / world / (peak_tf * 1e12),
+                            "kernel": kinfo})
+        if name != head:
+            continue
+        achieved_tf = FLOP_PER_PAIR * float(n) * n / (min(step_ms) * 1e-3) / 1e12
+        roofline = {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf,
+                    "unit": "TFLOP/s", "frac": achieved_tf / peak_tf,
+                    "traffic": traffic_from_profile(),
+                    "peak_source": "nominal: SMs x 128 FP32 lanes x 2 flop x max SM clock "
+                                   "(no FP32 peak in MEASURED_PEAKS.json)",
+                    "flop_per_pair": FLOP_PER_PAIR,
+                    "kernel_ms": {"min": min(step_ms), "median": statistics.median(step_ms)}}
+        # e2e through the C ABI with pinned host buffers
+        host = [torch.empty(n, dtype=torch.float32, pin_memory=True).numpy() for _ in range(6)]
+        for h, src in zip(host, pos + vel):
+            h[:] = src
+        e2e_steps = max(1, min(args.steps, 5))
+        sim.set_state(host[:3], host[3:])
         sim.advance(1)
-        sim.get_state(host)                 # 6 x N floats device -> host (synchronizes)
-    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
-    e2e = {"value": float(n) * n * e2e_steps * world / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": 6 * 4 * n, "d2h_bytes_per_step": 6 * 4 * n,
-           "ms_per_step": e2e_s * 1e3 / e2e_steps}
-
-    result = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded Plummer sphere generated by the library)",
-        "config": dict(workload_desc(n), kernel=kinfo, l2=(
-                           f"flushed between timed steps ({args.flush_mib} MiB write)"
-                           if args.flush_mib else "not flushed (profiling run)"),
-                       parallelism="replicas" if world > 1 else "single GPU"),
-        "gflops": value * FLOP_PER_PAIR / 1e9,
-        "fp32_peak_frac": value * FLOP_PER_PAIR / world / (peak_tf * 1e12),
-        "roofline": roofline, "e2e": e2e, "gpu_launches": args.steps,
-        "clocks": clk.summary(), "wall_s_timed_region": wall,
-    }
-    sim.close()
+        sim.get_state(host)
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            sim.set_state(host[:3], host[3:])   # 6 x N floats host -> device
+            sim.advance(1)
+            sim.get_state(host)                 # 6 x N floats device -> host (synchronizes)
+        e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+        e2e = {"value": float(n) * n * e2e_steps * world / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": 6 * 4 * n, "d2h_bytes_per_step": 6 * 4 * n,
+               "ms_per_step": e2e_s * 1e3 / e2e_steps}
+        result = {
+            "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Plummer sphere generated by the library)",
+            "config": dict(workload_desc(n), kernel=kinfo, accumulator=head, l2=(
+                f"flushed between timed steps ({args.flush_mib} MiB write)"
+                if args.flush_mib else "not flushed (profiling run)"),
+                parallelism="replicas" if world > 1 else "single GPU"),
+            "gflops": rate * FLOP_PER_PAIR / 1e9,
+            "fp32_peak_frac": rate * FLOP_PER_PAIR / world / (peak_tf * 1e12),
+            "force_rel_rms_vs_fp64": modes[head]["force_rel_rms_vs_fp64"],
+            "force_rel_max_vs_fp64": modes[head]["force_rel_max_vs_fp64"],
+            "roofline": roofline, "e2e": e2e, "gpu_launches": args.steps,
+            "clocks": clk.summary(), "wall_s_timed_region": wall,
+        }
+    result["accumulators"] = {k: {a: b for a, b in v.items() if a != "sim"}
+                              for k, v in modes.items()}
+    for v in modes.values():
+        v["sim"].close()
     del flush
     if rank == 0 and not args.no_extras:
         result["ensemble"] = bench_ensemble(args)
@@ -354,6 +400,61 @@ def bench_adjoint(args) -> dict:
             "note": "backward = recompute from checkpoints + VJP kernel, per step"}
 
 
+# --------------------------------------------------------------------------- precision study
+def run_precision_study(args) -> dict:
+    """Config 2: N = 262,144 two-disk collision, plain vs compensated FP32 accumulation.
+    FP64 energy and momenta (GPU) and the force error against FP64 accelerations on
+    sampled rows every `every` steps.  Damping is 1 so that energy is conserved by the
+    dynamics and its drift measures the arithmetic."""
+    import nbody_gb300 as nb
+
+    n, steps, every, eps, dt = args.n if args.n != N_BENCH else 262144, args.study_steps, 10, \
+        1e-3, 1e-3
+    (x, y, z), (vx, vy, vz), m = nb.two_disks(SEED, n, eps)
+    rows = np.linspace(0, n - 1, 2048).astype(np.uint64)
+    out = {"study": "precision", "N": n, "steps": steps, "every": every, "eps2": eps, "dt": dt,
+           "damping": 1.0, "G": 1.0, "seed": SEED, "rows_sampled": int(rows.size),
+           "modes": {}}
+    for name, acc in (("plain", nb.ACC_PLAIN), ("compensated", nb.ACC_COMPENSATED)):
+        p = nb.SimParam(numParticles=n, G=1.0, dt=dt, damping=1.0, distEps=eps, accumulator=acc)
+        sim = nb.Simulation(p, (x, y, z), (vx, vy, vz), m)
+        series = []
+        t_diag = t_step = 0.0
+        for k in range(0, steps + 1, every):
+            if k:
+                w = time.perf_counter()
+                sim.advance(every)
+                sim.synchronize()
+                t_step += time.perf_counter() - w
+            w = time.perf_counter()
+            d = sim.diagnostics()
+            a32 = sim.accelerations()
+            a64 = sim.fp64_accelerations(rows)
+            t_diag += time.perf_counter() - w
+            g = np.stack([a[rows.astype(np.int64)].astype(np.float64) for a in a32])
+            r = np.stack(a64)
+            err = np.linalg.norm(g - r, axis=0)
+            mag = np.linalg.norm(r, axis=0)
+            series.append({"step": k, "energy": d["total"], "kinetic": d["kinetic"],
+                           "potential": d["potential"], "momentum": d["momentum"],
+                           "angular_momentum": d["angular_momentum"],
+                           "force_rel_rms": float(np.sqrt(np.mean(err ** 2) / np.mean(mag ** 2))),
+                           "force_rel_max": float(np.max(err / np.maximum(mag, 1e-30)))})
+        e0 = series[0]["energy"]
+        p0 = np.array(series[0]["momentum"])
+        out["modes"][name] = {
+            "max_rel_energy_drift": max(abs(s_["energy"] - e0) / abs(e0) for s_ in series),
+            "final_rel_energy_drift": (series[-1]["energy"] - e0) / abs(e0),
+            "max_momentum_drift": max(float(np.linalg.norm(np.array(s_["momentum"]) - p0))
+                                      for s_ in series),
+            "force_rel_rms_mean": float(np.mean([s_["force_rel_rms"] for s_ in series])),
+            "force_rel_rms_max": float(np.max([s_["force_rel_rms"] for s_ in series])),
+            "force_rel_max_max": float(np.max([s_["force_rel_max"] for s_ in series])),
+            "seconds_stepping": t_step, "seconds_diagnostics": t_diag, "series": series}
+        sim.close()
+    return out
+
+
 # --------------------------------------------------------------------------- reference arm
 def run_reference(args, rank, world) -> dict | None:
     if rank != 0:
@@ -415,12 +516,23 @@ def main() -> int:
                     help="particles (default: the 1,048,576-particle workload; smaller values "
                          "are for profiling only)")
     ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--study", choices=["precision"], default=None,
+                    help="run a study instead of the benchmark (precision: config 2)")
+    ap.add_argument("--study-steps", type=int, default=1000)
     ap.add_argument("--flush-mib", type=int, default=512,
                     help="L2 flush buffer written between timed steps (0: no flush; profiling)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--acc", choices=["auto", "plain", "compensated"], default="auto",
+                    help="accumulator(s) to measure; auto: both, headline = plain if its force "
+                         "error vs FP64 is <= 1e-5 relative RMS, else compensated")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the FP64 force-error check (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)  # at least 3 untimed warm-up steps
+    if args.study == "precision":
+        print(json.dumps(run_precision_study(args)), flush=True)
+        return 0
     rank, world = dist_init()
     if args.impl == "reference":
         res = run_reference(args, rank, world)

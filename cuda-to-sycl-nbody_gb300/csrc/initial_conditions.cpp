@@ -93,7 +93,7 @@ extern "C" int nb_ic_plummer(uint64_t seed, uint64_t n, float* x, float* y, floa
     double X;
     do {
       X = unit(seed, i, k++);
-    } while (X > 0.999);
+    } while (X > 0.999 && k < 64);  // draws 0..63 only (64.. are the angles)
     const double r = 1.0 / std::sqrt(std::pow(X, -2.0 / 3.0) - 1.0);
     const double ct = 1.0 - 2.0 * unit(seed, i, 64);
     const double st = std::sqrt(std::max(0.0, 1.0 - ct * ct));
@@ -103,7 +103,7 @@ extern "C" int nb_ic_plummer(uint64_t seed, uint64_t n, float* x, float* y, floa
     pz[i] = r * ct;
     double q;
     uint64_t kk = 128;
-    while (true) {
+    for (int it = 0; it < 20000; ++it) {  // acceptance ~0.4: the bound is never reached
       q = unit(seed, i, kk);
       const double g = 0.1 * unit(seed, i, kk + 1);
       kk += 2;

@@ -58,6 +58,9 @@ struct AdjointArgs {
   const SystemDesc* sys;
   const int32_t* tile_sys;  // [tiles] system of each i-tile
   const int32_t* tile_idx;  // [tiles] i-tile index within its system
+  float4* partial;          // [num_splits][n_pad] per-chunk partial sums
+  int64_t n_pad;
+  int32_t num_splits;       // j-chunks per i-tile
   float eps2;
   float dt;
   int32_t mask_self;
@@ -74,5 +77,12 @@ cudaError_t launch_unpack_vec3(const float* in, int64_t n, const int64_t* map, f
                                cudaStream_t stream);
 cudaError_t launch_pack_vec3(const float4* in, int64_t n, const int64_t* map, float* out,
                              cudaStream_t stream);
+
+// ---- initial conditions on the device (initgen.cu) ------------------------------------
+// kind 1: thin disks, 2: Plummer (needs raw [6 * total] and mean [6 * nsys] FP64
+// scratch), 3: two-disk collisions.  first_d[k] = first user index of system k.
+cudaError_t launch_generate(int kind, float* pos, float4* vel, const SystemDesc* sys_d,
+                            const int64_t* first_d, int32_t nsys, int64_t total, uint64_t seed,
+                            double eps, double* raw, double* mean, cudaStream_t stream);
 
 }  // namespace nbg

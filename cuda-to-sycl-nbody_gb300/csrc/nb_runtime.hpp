@@ -43,6 +43,8 @@ struct AdjointState {
   int32_t* tile_sys = nullptr;
   int32_t* tile_idx = nullptr;
   int32_t num_tiles = 0;
+  int32_t num_splits = 1;
+  float4* partial = nullptr;        // [num_splits][n_pad]
   bool valid = false;
 };
 

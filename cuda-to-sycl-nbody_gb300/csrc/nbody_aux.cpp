@@ -29,6 +29,7 @@ void release_aux(nb_sim* s) {
   dev_free(a.vel);
   dev_free(a.tile_sys);
   dev_free(a.tile_idx);
+  dev_free(a.partial);
   a = AdjointState{};
 }
 
@@ -71,6 +72,10 @@ int ensure_adjoint_buffers(nb_sim* s, int32_t ncp, int32_t every) {
         ti.push_back(t);
       }
     a.num_tiles = static_cast<int32_t>(ts.size());
+    // j-chunks per i-tile: about 8 CTAs per SM in total, deterministic reduction after.
+    const int32_t target = 8 * s->sms;
+    a.num_splits = std::max(1, std::min(64, (target + a.num_tiles - 1) / a.num_tiles));
+    NB_TRY(dev_alloc(&a.partial, static_cast<size_t>(a.num_splits) * np));
     NB_TRY(dev_alloc(&a.tile_sys, ts.size()));
     NB_TRY(dev_alloc(&a.tile_idx, ti.size()));
     NB_CUDA(cudaMemcpy(a.tile_sys, ts.data(), ts.size() * sizeof(int32_t),
@@ -233,6 +238,9 @@ int nb_sim_adjoint_backward(nb_sim* s, const float* gx_T, const float* gv_T, flo
       aa.sys = s->sys_d;
       aa.tile_sys = a.tile_sys;
       aa.tile_idx = a.tile_idx;
+      aa.partial = a.partial;
+      aa.n_pad = s->n_pad;
+      aa.num_splits = a.num_splits;
       aa.eps2 = s->params.dist_eps;
       aa.dt = dt;
       aa.mask_self = s->mask_self;

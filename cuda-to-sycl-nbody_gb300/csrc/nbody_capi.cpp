@@ -297,14 +297,15 @@ int check_error_word(nb_sim* s) {
 }
 
 static int default_config(const nb_sim* s) {
-  // Large systems: 512-particle i-tiles; many small systems: 256-particle i-tiles.
+  // Large systems: 256 x 4 (1024-particle i-tiles, one CTA per SM); ensembles of
+  // small systems: 256 x 2.
   int64_t sum_n2 = 0, sum_n3 = 0;
   for (const auto& d : s->sys_h) {
     sum_n2 += static_cast<int64_t>(d.n) * d.n;
     sum_n3 += static_cast<int64_t>(d.n) * d.n / 64 * d.n / 64;
   }
   const double weighted_n = sum_n2 ? static_cast<double>(sum_n3) * 4096.0 / sum_n2 : 0.0;
-  return weighted_n >= 16384.0 ? 0 : 3;
+  return weighted_n >= 16384.0 ? 1 : 3;
 }
 
 static int create_impl(const nb_params* p, uint32_t num_systems, const uint32_t* sizes, const float* x,
@@ -789,6 +790,49 @@ int nb_plan_work(uint32_t num_systems, const uint32_t* sizes, int32_t config_ind
   }
   if (seg_begin) std::memcpy(seg_begin, h.seg_begin.data(), h.seg_begin.size() * sizeof(int32_t));
   return NB_OK;
+}
+
+int nb_sim_generate(nb_sim* s, int32_t kind, uint64_t seed) {
+  if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  if (kind != NB_IC_THIN_DISK && kind != NB_IC_PLUMMER && kind != NB_IC_TWO_DISKS)
+    return set_error(NB_ERR_INVALID_ARGUMENT, "unknown initial-condition kind");
+  const int32_t nsys = static_cast<int32_t>(s->sys_h.size());
+  std::vector<float> m(s->n_real);
+  for (int32_t k = 0; k < nsys; ++k) {
+    const int32_t n = s->sys_h[k].n;
+    if (kind == NB_IC_TWO_DISKS && (n < 2 || n % 2))
+      return set_error(NB_ERR_INVALID_ARGUMENT, "two-disk systems need an even size");
+    const double per = kind == NB_IC_TWO_DISKS ? 1.0 / (n / 2) : 1.0 / n;
+    std::fill(m.begin() + s->user_offset[k], m.begin() + s->user_offset[k] + n,
+              static_cast<float>(per));
+  }
+  int64_t* first_d = nullptr;
+  double* raw = nullptr;
+  double* mean = nullptr;
+  int st = dev_alloc(&first_d, static_cast<size_t>(nsys));
+  if (st == NB_OK && kind == NB_IC_PLUMMER) st = dev_alloc(&raw, 6 * s->n_real);
+  if (st == NB_OK && kind == NB_IC_PLUMMER) st = dev_alloc(&mean, 6 * static_cast<size_t>(nsys));
+  cudaError_t e = cudaSuccess;
+  if (st == NB_OK) {
+    e = cudaMemcpyAsync(first_d, s->user_offset.data(), nsys * sizeof(int64_t),
+                        cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess)
+      e = launch_generate(kind, s->pos_d[s->cur], s->vel_d, s->sys_d, first_d, nsys,
+                          static_cast<int64_t>(s->n_real), seed, s->params.dist_eps, raw, mean,
+                          s->stream);
+    // Both buffers carry the masses.
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(s->pos_d[s->cur ^ 1], s->pos_d[s->cur], 4 * sizeof(float) * s->n_pad,
+                          cudaMemcpyDeviceToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  }
+  dev_free(first_d);
+  dev_free(raw);
+  dev_free(mean);
+  if (st != NB_OK) return st;
+  if (e != cudaSuccess) return cuda_error(e, "generate initial conditions");
+  assign_mass_mode(s, m);
+  return upload_systems(s) == NB_OK ? check_error_word(s) : NB_ERR_CUDA;
 }
 
 int nb_sim_inject_wait_timeout(nb_sim* s) {

@@ -32,6 +32,9 @@ BRANCH = 0
 PREDICATED = 1
 ACC_PLAIN = 0
 ACC_COMPENSATED = 1
+IC_THIN_DISK = 1
+IC_PLUMMER = 2
+IC_TWO_DISKS = 3
 
 
 class NbError(RuntimeError):
@@ -101,6 +104,7 @@ SIGNATURES = {
     "nb_sim_advance_per_system": (C.c_int, [_P, C.c_int32]),
     "nb_sim_synchronize": (C.c_int, [_P]),
     "nb_sim_inject_wait_timeout": (C.c_int, [_P]),
+    "nb_sim_generate": (C.c_int, [_P, C.c_int32, C.c_uint64]),
     "nb_sim_time_iterations": (C.c_int, [_P, C.c_int32, C.c_int32, _F]),
     "nb_sim_get_state": (C.c_int, [_P] + [_F] * 6),
     "nb_sim_set_state": (C.c_int, [_P] + [_F] * 7),
@@ -382,6 +386,10 @@ class Simulation:
             arrs[3:6] = [_f32(a, self.n) for a in vel]
         m = None if mass is None else _f32(mass, self.n)
         _check(lib.nb_sim_set_state(self._h, *[_fp(a) for a in arrs], _fp(m)))
+
+    def generate(self, kind: int, seed: int) -> None:
+        """Regenerate every system's state on the GPU (system k uses seed + k)."""
+        _check(lib.nb_sim_generate(self._h, kind, seed))
 
     def accelerations(self):
         o = [np.empty(self.n, dtype=np.float32) for _ in range(3)]

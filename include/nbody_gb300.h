@@ -255,6 +255,17 @@ int nb_sim_adjoint_backward(nb_sim* s, const float* gx_T, const float* gv_T,
 int nb_accelerations_noalloc(const float* pos_xyzm_device, uint64_t n, float G, float dist_eps,
                              float* accel_xyzw_device, void* stream);
 
+/* ---- initial conditions on the device ---------------------------------------------- */
+typedef enum nb_ic_kind { NB_IC_THIN_DISK = 1, NB_IC_PLUMMER = 2, NB_IC_TWO_DISKS = 3 } nb_ic_kind;
+/* Overwrite the state of every system with seeded initial conditions generated on
+ * the GPU, directly in the device layout (the reference can only generate on the
+ * host and copy, simulator.cu:77-103).  System k uses seed + k and gets the same
+ * draws as the host generator below with that seed (values can differ from the
+ * host's by one float rounding).  Thin disks use the simulation's dist_eps;
+ * NB_IC_TWO_DISKS needs even system sizes.  Masses become 1/n per system (1/(n/2)
+ * for two disks). */
+int nb_sim_generate(nb_sim* s, int32_t kind, uint64_t seed);
+
 /* ---- initial conditions (host, seeded, deterministic) -------------------------------- */
 /* Thin disk: r = sqrt(u), theta uniform, z ~ N(0, 0.01^2), tangential speed
  * r * sqrt(n m r^2 / (r^2 + eps)^1.5) + N(0, 0.01) per component, m = 1/n. */
