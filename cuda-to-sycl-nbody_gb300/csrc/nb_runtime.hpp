@@ -10,6 +10,7 @@
 
 #include "nb_internal.hpp"
 #include "nb_kernels.hpp"
+#include "nb_render.hpp"
 #include "nbody_gb300.h"
 
 namespace nbg {
@@ -94,6 +95,7 @@ struct nb_sim {
   nbg::DiagScratch diag{};
   double* diag_out_d = nullptr;
   nbg::AdjointState adj;
+  nbg::RenderBuffers render;
 };
 
 namespace nbg {
@@ -105,6 +107,7 @@ int check_device(int* sms, cudaDeviceProp* prop);
 void free_worklist(WorkListDev& w);
 // Free the diagnostics and adjoint buffers of a simulation.
 void release_aux(nb_sim* s);
+void release_render_buffers(nb_sim* s);
 
 template <class T>
 int dev_alloc(T** p, size_t count) {

@@ -545,6 +545,7 @@ int nb_sim_destroy(nb_sim* s) {
   dev_free(s->partials_d);
   dev_free(s->counters_d);
   release_aux(s);
+  release_render_buffers(s);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);

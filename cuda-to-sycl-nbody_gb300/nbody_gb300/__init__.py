@@ -105,6 +105,10 @@ SIGNATURES = {
     "nb_sim_synchronize": (C.c_int, [_P]),
     "nb_sim_inject_wait_timeout": (C.c_int, [_P]),
     "nb_sim_generate": (C.c_int, [_P, C.c_int32, C.c_uint64]),
+    "nb_camera_matrices": (C.c_int, [C.c_float, C.c_float, C.c_float, _F, C.c_int32, C.c_int32,
+                                     _F, _F]),
+    "nb_render_tables": (C.c_int, [_F, _F, _I32, _F]),
+    "nb_sim_render": (C.c_int, [_P, _F, _F, C.c_int32, C.c_int32, _P]),
     "nb_sim_time_iterations": (C.c_int, [_P, C.c_int32, C.c_int32, _F]),
     "nb_sim_get_state": (C.c_int, [_P] + [_F] * 6),
     "nb_sim_set_state": (C.c_int, [_P] + [_F] * 7),
@@ -251,6 +255,28 @@ def accelerations_noalloc(pos_xyzm_ptr: int, n: int, G: float, dist_eps: float,
                                         C.c_void_p(stream_ptr) if stream_ptr else None))
 
 
+def camera_matrices(azimuth: float, elevation: float, distance: float, width: int, height: int,
+                    look_at=(0.0, 0.0, 0.0)):
+    """(view, proj) as 4x4 column-major float32 arrays (flattened, OpenGL order)."""
+    view = np.empty(16, np.float32)
+    proj = np.empty(16, np.float32)
+    at = np.asarray(look_at, np.float32)
+    _check(lib.nb_camera_matrices(azimuth, elevation, distance, at.ctypes.data_as(_F), width,
+                                  height, view.ctypes.data_as(_F), proj.ctypes.data_as(_F)))
+    return view, proj
+
+
+def render_tables():
+    """(gauss offsets, gauss weights, flare 16x16) of the renderer."""
+    off = np.zeros(32, np.float32)
+    w = np.zeros(32, np.float32)
+    taps = C.c_int32()
+    flare = np.zeros(256, np.float32)
+    _check(lib.nb_render_tables(off.ctypes.data_as(_F), w.ctypes.data_as(_F), C.byref(taps),
+                                flare.ctypes.data_as(_F)))
+    return off[:taps.value], w[:taps.value], flare.reshape(16, 16)
+
+
 # ---------------------------------------------------------------------------- initial conditions
 def _ic_out(n: int):
     return [np.empty(n, dtype=np.float32) for _ in range(7)]
@@ -395,6 +421,13 @@ class Simulation:
         o = [np.empty(self.n, dtype=np.float32) for _ in range(3)]
         _check(lib.nb_sim_accelerations(self._h, *[_fp(a) for a in o]))
         return o
+
+    def render(self, view, proj, width: int, height: int, rgba_ptr: int) -> None:
+        """Render into a width x height float4 device buffer (row 0 at the bottom)."""
+        v = np.ascontiguousarray(view, np.float32)
+        p = np.ascontiguousarray(proj, np.float32)
+        _check(lib.nb_sim_render(self._h, v.ctypes.data_as(_F), p.ctypes.data_as(_F), width,
+                                 height, C.c_void_p(rgba_ptr)))
 
     def export_device(self, pos_ptr: int, vel_ptr: int | None = None) -> None:
         _check(lib.nb_sim_export_device(self._h, C.c_void_p(pos_ptr),

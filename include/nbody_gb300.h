@@ -255,6 +255,26 @@ int nb_sim_adjoint_backward(nb_sim* s, const float* gx_T, const float* gv_T,
 int nb_accelerations_noalloc(const float* pos_xyzm_device, uint64_t n, float G, float dist_eps,
                              float* accel_xyzw_device, void* stream);
 
+/* ---- headless render math ---------------------------------------------------------- */
+/* Camera matrices of the reference's orbit camera (Camera::getView / getProj,
+ * camera.cpp:38-52): eye at distance `distance` from `look_at` (NULL = origin) at
+ * the given azimuth and elevation (radians), z up; infinite perspective, fovy 30
+ * degrees, near 1, aspect width / height.  Column-major 4x4, as OpenGL. */
+int nb_camera_matrices(float azimuth, float elevation, float distance, const float look_at[3],
+                       int32_t width, int32_t height, float view[16], float proj[16]);
+/* The renderer's fixed tables: the 13 merged Gaussian blur taps (sigma 10, 25
+ * taps; RendererGL::gaussKernel/optimGaussKernel, renderer_gl.cpp:314-368) and the
+ * 16 x 16 flare texture (genFlareTex, gen.cpp:36-51). */
+int nb_render_tables(float* gauss_offsets, float* gauss_weights, int32_t* taps, float* flare);
+/* Render the current state as the reference's OpenGL renderer does
+ * (RendererGL::render, renderer_gl.cpp:96-157; shaders/gl/*): additive
+ * velocity-coloured flare sprites into an HDR buffer with a 50-pixel margin,
+ * half-resolution separable Gaussian bloom, mean luminance, exposure tonemap and
+ * gamma 2.2 -- on the GPU, with no graphics API.  Writes width x height float4
+ * RGBA (row 0 at the bottom) to `rgba_device`.  Stream-ordered. */
+int nb_sim_render(nb_sim* s, const float view[16], const float proj[16], int32_t width,
+                  int32_t height, float* rgba_device);
+
 /* ---- initial conditions on the device ---------------------------------------------- */
 typedef enum nb_ic_kind { NB_IC_THIN_DISK = 1, NB_IC_PLUMMER = 2, NB_IC_TWO_DISKS = 3 } nb_ic_kind;
 /* Overwrite the state of every system with seeded initial conditions generated on

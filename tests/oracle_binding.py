@@ -42,6 +42,9 @@ def lib() -> C.CDLL:
                                                                   C.c_int64] + [_D] * 3
         L.oracle_energy_fp64.argtypes = [C.c_int64] + [_F] * 7 + [C.c_double, C.c_double, _D]
         L.oracle_num_threads.restype = C.c_int
+        L.oracle_render.argtypes = [C.c_int64] + [_F] * 7 + [C.c_int, C.c_int, _F, _F, C.c_int,
+                                                              _F, C.c_int, _F]
+        L.oracle_render.restype = C.c_int
         _lib = L
     return _lib
 
@@ -103,6 +106,21 @@ def energy_fp64(pos, vel, mass, G, eps) -> dict:
                              out.ctypes.data_as(_D))
     return {"kinetic": out[0], "potential": out[1], "total": out[0] + out[1],
             "momentum": list(out[2:5]), "angular_momentum": list(out[5:8]), "mass": out[8]}
+
+
+def render(pos, vel, pv, width, height, offsets, weights, flare):
+    """CPU restatement of the reference's render math; (height, width, 4) float32."""
+    x, y, z = (_f(a) for a in pos)
+    vx, vy, vz = (_f(a) for a in vel)
+    pvm = _f(pv)
+    off, wt, fl = _f(offsets), _f(weights), _f(flare)
+    out = np.zeros((height, width, 4), np.float32)
+    rc = lib().oracle_render(x.size, _p(x), _p(y), _p(z), _p(vx), _p(vy), _p(vz), _p(pvm), width,
+                             height, _p(off), _p(wt), off.size, _p(fl), int(round(fl.size ** 0.5)),
+                             _p(out))
+    if rc != 0:
+        raise MemoryError("oracle_render")
+    return out
 
 
 # ------------------------------------------------------------------ reference kernel
