@@ -23,7 +23,6 @@ from __future__ import annotations
 
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -137,14 +136,6 @@ def max_over_ranks(v: float, world: int) -> float:
     t = torch.tensor([v], dtype=torch.float64, device="cuda")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
-
-
-def peaks() -> dict:
-    p = ROOT / "MEASURED_PEAKS.json"
-    try:
-        return json.loads(p.read_text())
-    except (OSError, ValueError):
-        return {}
 
 
 def cpu_sample_rate(pos, mass_G, target_s: float, max_rows: int | None = None):
@@ -492,6 +483,45 @@ def run_precision_study(args) -> dict:
     return out
 
 
+# --------------------------------------------------------------------------- accuracy study
+def run_accuracy_study(args) -> dict:
+    """Force error of both accumulators against FP64 for the initial state of each
+    configuration: FP32 accelerations of the library vs GPU FP64 accelerations on
+    strided rows (for the ensemble: rows spread over all systems)."""
+    import nbody_gb300 as nb
+
+    cases = []
+    (x, y, z), (vx, vy, vz), m = nb.thin_disk(SEED, 25600, 1e-3)
+    cases.append(("config0_disk_25600", [x, y, z], [vx, vy, vz], m, None, 1e-3))
+    (x, y, z), (vx, vy, vz), m = nb.plummer(SEED, 1 << 20)
+    cases.append(("config1_plummer_1048576", [x, y, z], [vx, vy, vz], m, None, 1e-4))
+    (x, y, z), (vx, vy, vz), m = nb.two_disks(SEED, 262144, 1e-3)
+    cases.append(("config2_two_disks_262144", [x, y, z], [vx, vy, vz], m, None, 1e-3))
+    sizes = nb.ensemble_sizes(SEED, 4096, 64, 8192)
+    parts = [nb.plummer(SEED + 1 + k, int(s_)) for k, s_ in enumerate(sizes)]
+    cases.append(("config3_ensemble_4096_systems",
+                  [np.concatenate([q[0][c] for q in parts]) for c in range(3)],
+                  [np.concatenate([q[1][c] for q in parts]) for c in range(3)],
+                  np.concatenate([q[2] for q in parts]), sizes, 1e-3))
+    (x, y, z), (vx, vy, vz), m = nb.thin_disk(SEED, 16384, 1e-3)
+    cases.append(("config4_disk_16384", [x, y, z], [vx, vy, vz], m, None, 1e-3))
+    out = {"study": "accuracy", "rows": 2048, "reference": "GPU FP64 all-pairs rows "
+           "(nb_sim_fp64_accelerations), checked against the CPU FP64 oracle in the tests",
+           "cases": {}}
+    for name, pos, vel, m, sizes_, eps in cases:
+        n = pos[0].size
+        res = {"N": int(n), "eps2": eps}
+        for acc_name, acc in (("plain", nb.ACC_PLAIN), ("compensated", nb.ACC_COMPENSATED)):
+            p = nb.SimParam(G=1.0, dt=1e-3, damping=1.0, distEps=eps, accumulator=acc,
+                            numParticles=n)
+            sim = nb.Simulation(p, pos, vel, m, sizes=sizes_)
+            rms, mx, rows = force_error_vs_fp64(sim, n, 2048)
+            res[acc_name] = {"force_rel_rms_vs_fp64": rms, "force_rel_max_vs_fp64": mx}
+            sim.close()
+        out["cases"][name] = res
+    return out
+
+
 # --------------------------------------------------------------------------- reference arm
 def run_reference(args, rank, world) -> dict | None:
     if rank != 0:
@@ -553,8 +583,9 @@ def main() -> int:
                     help="particles (default: the 1,048,576-particle workload; smaller values "
                          "are for profiling only)")
     ap.add_argument("--autotune", action="store_true")
-    ap.add_argument("--study", choices=["precision"], default=None,
-                    help="run a study instead of the benchmark (precision: config 2)")
+    ap.add_argument("--study", choices=["precision", "accuracy"], default=None,
+                    help="run a study instead of the benchmark (precision: config 2 over time; "
+                         "accuracy: force error vs FP64 of every config, both accumulators)")
     ap.add_argument("--study-steps", type=int, default=1000)
     ap.add_argument("--flush-mib", type=int, default=512,
                     help="L2 flush buffer written between timed steps (0: no flush; profiling)")
@@ -569,6 +600,9 @@ def main() -> int:
     args.warmup = max(3, args.warmup)  # at least 3 untimed warm-up steps
     if args.study == "precision":
         print(json.dumps(run_precision_study(args)), flush=True)
+        return 0
+    if args.study == "accuracy":
+        print(json.dumps(run_accuracy_study(args)), flush=True)
         return 0
     rank, world = dist_init()
     if args.impl == "reference":

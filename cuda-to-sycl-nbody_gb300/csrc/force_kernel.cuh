@@ -145,18 +145,19 @@ __device__ __forceinline__ void kahan_finish(float2 s, float2 c, float& hi, floa
   lo = e - (c.x + c.y);
 }
 
-// Pair loop over `npairs` j-pairs of one shared-memory tile (npairs % 8 == 0).
+// Pair loop over `npairs` j-pairs of one shared-memory tile (npairs % 8 == 0), U
+// j-pairs per unrolled step.
 // kMask: zero the term of j == i (tiles overlapping the i-tile when eps2^3 underflows).
-template <int R, bool kMass, bool kMask>
+template <int R, int U, bool kMass, bool kMask>
 __device__ __forceinline__ void tile_pairs(const float4* __restrict__ tile, int npairs, float2 e2,
                                            const float2 (&nx)[R], const float2 (&ny)[R],
                                            const float2 (&nz)[R], float2 (&ax)[R],
                                            float2 (&ay)[R], float2 (&az)[R], int64_t j_first,
                                            const int64_t (&gi)[R]) {
 #pragma unroll 1
-  for (int p = 0; p < npairs; p += 4) {
+  for (int p = 0; p < npairs; p += U) {
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < U; ++u) {
       const float4 A = tile[2 * (p + u)];
       const float4 B = tile[2 * (p + u) + 1];
       const float2 xx = make_float2(A.x, A.y);
@@ -191,7 +192,7 @@ __device__ __forceinline__ void tile_pairs(const float4* __restrict__ tile, int 
 // to 255 registers per thread for the R i-particles and the unrolled pair loop (with
 // the thread bound alone it caps 256-thread shapes at 128 registers, measured 17 %
 // slower).
-template <int THREADS, int R, int BJ, int STAGES, bool kComp, bool kMass>
+template <int THREADS, int R, int BJ, int STAGES, int U, bool kComp, bool kMass>
 __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
   constexpr int BI = THREADS * R;
   constexpr int TILE_BYTES = BJ * 16;
@@ -278,9 +279,9 @@ __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
       const int64_t j_first = sd.offset + static_cast<int64_t>(jt) * BJ;
       const bool diag = a.mask_self && (jt * BJ < ibase + BI) && (ibase < jt * BJ + count);
       if (diag) {
-        tile_pairs<R, kMass, true>(tile, count >> 1, e2, nx, ny, nz, ax, ay, az, j_first, gi);
+        tile_pairs<R, U, kMass, true>(tile, count >> 1, e2, nx, ny, nz, ax, ay, az, j_first, gi);
       } else {
-        tile_pairs<R, kMass, false>(tile, count >> 1, e2, nx, ny, nz, ax, ay, az, j_first, gi);
+        tile_pairs<R, U, kMass, false>(tile, count >> 1, e2, nx, ny, nz, ax, ay, az, j_first, gi);
       }
       if (kComp) {
 #pragma unroll
@@ -394,29 +395,29 @@ __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
   }
 }
 
-template <int T, int R, int BJ, int S, bool C, bool M>
+template <int T, int R, int BJ, int S, int U, bool C, bool M>
 cudaError_t launch_one(const ForceArgs& a, int grid, cudaStream_t st) {
   constexpr int smem = S * BJ * 16;
-  force_kernel<T, R, BJ, S, C, M><<<grid, T, smem, st>>>(a);
+  force_kernel<T, R, BJ, S, U, C, M><<<grid, T, smem, st>>>(a);
   return cudaGetLastError();
 }
 
-template <int T, int R, int BJ, int S, bool C, bool M>
+template <int T, int R, int BJ, int S, int U, bool C, bool M>
 cudaError_t occ_one(int* blocks) {
   constexpr int smem = S * BJ * 16;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, force_kernel<T, R, BJ, S, C, M>,
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, force_kernel<T, R, BJ, S, U, C, M>,
                                                        T, smem);
 }
 
 }  // namespace
 
-#define NBG_CONFIG(T, R, BJ, S)                                                            \
+#define NBG_CONFIG(T, R, BJ, S, U)                                                          \
   ConfigEntry {                                                                            \
     KernelShape{T, R, BJ, S},                                                              \
-        {{launch_one<T, R, BJ, S, false, false>, launch_one<T, R, BJ, S, false, true>},    \
-         {launch_one<T, R, BJ, S, true, false>, launch_one<T, R, BJ, S, true, true>}},     \
-        {{occ_one<T, R, BJ, S, false, false>, occ_one<T, R, BJ, S, false, true>},          \
-         {occ_one<T, R, BJ, S, true, false>, occ_one<T, R, BJ, S, true, true>}},           \
+        {{launch_one<T, R, BJ, S, U, false, false>, launch_one<T, R, BJ, S, U, false, true>}, \
+         {launch_one<T, R, BJ, S, U, true, false>, launch_one<T, R, BJ, S, U, true, true>}},  \
+        {{occ_one<T, R, BJ, S, U, false, false>, occ_one<T, R, BJ, S, U, false, true>},       \
+         {occ_one<T, R, BJ, S, U, true, false>, occ_one<T, R, BJ, S, U, true, true>}},        \
   }
 
 }  // namespace nbg

@@ -5,10 +5,10 @@
 namespace nbg {
 
 extern const ConfigEntry kForceShapesA[] = {
-    NBG_CONFIG(128, 4, 256, 3),
-    NBG_CONFIG(256, 4, 256, 3),
-    NBG_CONFIG(128, 8, 256, 3),
-    NBG_CONFIG(256, 2, 256, 3),
+    NBG_CONFIG(128, 4, 256, 3, 4),
+    NBG_CONFIG(256, 4, 256, 3, 4),
+    NBG_CONFIG(128, 8, 256, 3, 4),
+    NBG_CONFIG(256, 2, 256, 3, 4),
 };
 extern const int kNumForceShapesA = sizeof(kForceShapesA) / sizeof(kForceShapesA[0]);
 
