@@ -128,14 +128,21 @@ def barrier(world):
 
 
 def max_over_ranks(v: float, world: int) -> float:
+    """The largest of every rank's `v` (the whole job's time is the slowest rank's)."""
     if world == 1:
         return v
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, seconds_this_rank: float, world: int) -> float:
+    """Units processed by all ranks divided by the slowest rank's time."""
+    return units_per_rank * world / max_over_ranks(seconds_this_rank, world)
 
 
 def cpu_sample_rate(pos, mass_G, target_s: float, max_rows: int | None = None):

@@ -1,0 +1,56 @@
+"""The benchmark's multi-rank path on CPU: world size 2 over gloo (127.0.0.1).
+With N GPUs the benchmark runs N independent replicas; the whole-job rate is
+all ranks' pair interactions over the slowest rank's time."""
+from __future__ import annotations
+
+import os
+import socket
+import sys
+from pathlib import Path
+
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.distributed as dist  # noqa: E402
+import torch.multiprocessing as mp  # noqa: E402
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank: int, world: int, port: int, q) -> None:
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE=str(world), NB_BENCH_BACKEND="gloo")
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    r, w = bench.dist_init()
+    try:
+        slowest = bench.max_over_ranks(1.0 + r, w)
+        rate = bench.whole_job_rate(1000.0, 2.0 + 2 * r, w)
+        bench.barrier(w)
+        q.put((r, w, slowest, rate))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_aggregate_like_the_benchmark():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert [o[:2] for o in out] == [(0, 2), (1, 2)]
+    for _, _, slowest, rate in out:
+        assert slowest == 2.0                     # max over ranks
+        assert rate == pytest.approx(2 * 1000.0 / 4.0)
