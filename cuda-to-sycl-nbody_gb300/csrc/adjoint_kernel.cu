@@ -5,6 +5,7 @@
 //   F_i(x) = sum_{j != i} m_j r_ij f(|r_ij|^2 + eps),  r_ij = x_j - x_i,  f(s) = s^(-3/2).
 // Given the cotangents (lx', lv') of (x', v'):
 //   mu = lv' + dt lx',   lv = d mu,   lx = lx' + dt G J(x)^T mu,
+// (mu is formed where it is read; lx and lv are written by the combining pass),
 // and, with K_ij = s_ij I - 3 q_ij r_ij r_ij^T (s = f, q = s / (r^2 + eps)), which is
 // symmetric in i and j,
 //   (J^T mu)_i = sum_{j != i} K_ij u_ij,  u_ij = m_i mu_j - m_j mu_i
@@ -107,7 +108,9 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_partial_kernel(const Adjo
     const int64_t g = sd.offset + (li[r] < sd.n ? li[r] : sd.n - 1);
     const float x = a.pos[pair_index(g, 0)], y = a.pos[pair_index(g, 1)],
                 z = a.pos[pair_index(g, 2)], m = a.pos[pair_index(g, 3)];
-    const float4 mu = a.mu[g];
+    const float4 lx = a.lam_x[g], lv = a.lam_v[g];  // mu = lv' + dt lx'
+    const float4 mu = make_float4(fmaf(a.dt, lx.x, lv.x), fmaf(a.dt, lx.y, lv.y),
+                                  fmaf(a.dt, lx.z, lv.z), 0.f);
     nx[r] = f2(-x, -x);
     ny[r] = f2(-y, -y);
     nz[r] = f2(-z, -z);
@@ -129,7 +132,9 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_partial_kernel(const Adjo
         const int lj = j0 + 2 * p + h;
         if (2 * p + h < cnt) {
           const int64_t gj = sd.offset + lj;
-          const float4 mu = a.mu[gj];
+          const float4 lx = a.lam_x[gj], lv = a.lam_v[gj];
+          const float4 mu = make_float4(fmaf(a.dt, lx.x, lv.x), fmaf(a.dt, lx.y, lv.y),
+                                        fmaf(a.dt, lx.z, lv.z), 0.f);
           v[h][0] = a.pos[pair_index(gj, 0)];
           v[h][1] = a.pos[pair_index(gj, 1)];
           v[h][2] = a.pos[pair_index(gj, 2)];
@@ -168,7 +173,8 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_partial_kernel(const Adjo
   }
 }
 
-// lx = lx' + dt * gscale * sum over chunks (in chunk order), real particles only.
+// lx = lx' + dt * gscale * sum over chunks (in chunk order) and lv = damping * mu,
+// real particles only.
 __global__ void adjoint_combine_kernel(const AdjointArgs a) {
   const SystemDesc sd = a.sys[a.tile_sys[blockIdx.x]];
   const int ibase = a.tile_idx[blockIdx.x] * kAdjBI;
@@ -184,26 +190,10 @@ __global__ void adjoint_combine_kernel(const AdjointArgs a) {
       sy += p.y;
       sz += p.z;
     }
-    const float4 l = a.lam_x[g];
+    const float4 l = a.lam_x[g], v = a.lam_v[g];
     a.lam_x_out[g] = make_float4(fmaf(c, sx, l.x), fmaf(c, sy, l.y), fmaf(c, sz, l.z), 0.f);
-  }
-}
-
-__global__ void prepare_kernel(const float4* __restrict__ lx, const float4* __restrict__ lv,
-                               float4* __restrict__ mu, float dt, int64_t n) {
-  for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < n;
-       g += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const float4 a = lx[g], b = lv[g];
-    mu[g] = make_float4(fmaf(dt, a.x, b.x), fmaf(dt, a.y, b.y), fmaf(dt, a.z, b.z), 0.f);
-  }
-}
-
-__global__ void finish_v_kernel(const float4* __restrict__ mu, float4* __restrict__ lv,
-                                float damping, int64_t n) {
-  for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < n;
-       g += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const float4 m = mu[g];
-    lv[g] = make_float4(damping * m.x, damping * m.y, damping * m.z, 0.f);
+    a.lam_v_out[g] = make_float4(a.damping * fmaf(a.dt, l.x, v.x), a.damping * fmaf(a.dt, l.y, v.y),
+                                 a.damping * fmaf(a.dt, l.z, v.z), 0.f);
   }
 }
 
@@ -247,18 +237,6 @@ cudaError_t launch_adjoint(const AdjointArgs& a, int32_t num_tiles, bool per_pai
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   adjoint_combine_kernel<<<num_tiles, 256, 0, stream>>>(a);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_adjoint_prepare(const float4* lam_x, const float4* lam_v, float4* mu,
-                                   float dt, int64_t n_pad, cudaStream_t stream) {
-  prepare_kernel<<<grid_for(n_pad), 256, 0, stream>>>(lam_x, lam_v, mu, dt, n_pad);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_adjoint_finish_v(const float4* mu, float4* lam_v_out, float damping,
-                                    int64_t n_pad, cudaStream_t stream) {
-  finish_v_kernel<<<grid_for(n_pad), 256, 0, stream>>>(mu, lam_v_out, damping, n_pad);
   return cudaGetLastError();
 }
 

@@ -52,9 +52,10 @@ cudaError_t launch_fp64_rows(const float* pos, const SystemDesc* sys_d, const in
 // ---- adjoint (adjoint_kernel.cu) ----------------------------------------------------
 struct AdjointArgs {
   const float* pos;       // pair layout, positions x_t at which the Jacobian is taken
-  const float4* mu;       // [n_pad] adjoint vector mu = lam_v' + dt lam_x' (w unused)
-  const float4* lam_x;    // [n_pad] lam_x'
-  float4* lam_x_out;      // [n_pad] lam_x = lam_x' + dt * G * J^T mu
+  const float4* lam_x;    // [n_pad] lam_x' (cotangent of x')
+  const float4* lam_v;    // [n_pad] lam_v' (cotangent of v')
+  float4* lam_x_out;      // [n_pad] lam_x = lam_x' + dt * G * J^T mu, mu = lam_v' + dt lam_x'
+  float4* lam_v_out;      // [n_pad] lam_v = damping * mu
   const SystemDesc* sys;
   const int32_t* tile_sys;  // [tiles] system of each i-tile
   const int32_t* tile_idx;  // [tiles] i-tile index within its system
@@ -63,15 +64,12 @@ struct AdjointArgs {
   int32_t num_splits;       // j-chunks per i-tile
   float eps2;
   float dt;
+  float damping;
   int32_t mask_self;
 };
 cudaError_t launch_adjoint(const AdjointArgs& a, int32_t num_tiles, bool per_pair_mass,
                            cudaStream_t stream);
 int adjoint_tile();  // i-particles per adjoint CTA
-cudaError_t launch_adjoint_prepare(const float4* lam_x, const float4* lam_v, float4* mu,
-                                   float dt, int64_t n_pad, cudaStream_t stream);
-cudaError_t launch_adjoint_finish_v(const float4* mu, float4* lam_v_out, float damping,
-                                    int64_t n_pad, cudaStream_t stream);
 // n x 3 interleaved (user order) <-> padded float4.
 cudaError_t launch_unpack_vec3(const float* in, int64_t n, const int64_t* map, float4* out,
                                cudaStream_t stream);

@@ -204,6 +204,7 @@ int nb_sim_adjoint_backward(nb_sim* s, const float* gx_T, const float* gv_T, flo
   NB_CUDA(cudaMemsetAsync(a.lam_x, 0, np * sizeof(float4), s->stream));
   NB_CUDA(cudaMemsetAsync(a.lam_v, 0, np * sizeof(float4), s->stream));
   NB_CUDA(cudaMemsetAsync(a.tmp, 0, np * sizeof(float4), s->stream));
+  NB_CUDA(cudaMemsetAsync(a.mu, 0, np * sizeof(float4), s->stream));
   NB_CUDA(cudaMemcpyAsync(stage, gx_T, 3 * n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
   NB_CUDA(launch_unpack_vec3(stage, n, s->map_d, a.lam_x, s->stream));
   if (gv_T) {
@@ -229,12 +230,12 @@ int nb_sim_adjoint_backward(nb_sim* s, const float* gx_T, const float* gv_T, flo
     }
     // Reverse through the segment.
     for (int32_t t = L - 1; t >= 0; --t) {
-      NB_CUDA(launch_adjoint_prepare(a.lam_x, a.lam_v, a.mu, dt, s->n_pad, s->stream));
       AdjointArgs aa{};
       aa.pos = a.seg_pos[t];
-      aa.mu = a.mu;
       aa.lam_x = a.lam_x;
+      aa.lam_v = a.lam_v;
       aa.lam_x_out = a.tmp;
+      aa.lam_v_out = a.mu;  // second buffer pair: (tmp, mu) <- (lam_x, lam_v)
       aa.sys = s->sys_d;
       aa.tile_sys = a.tile_sys;
       aa.tile_idx = a.tile_idx;
@@ -243,10 +244,11 @@ int nb_sim_adjoint_backward(nb_sim* s, const float* gx_T, const float* gv_T, flo
       aa.num_splits = a.num_splits;
       aa.eps2 = s->params.dist_eps;
       aa.dt = dt;
+      aa.damping = s->params.damping;
       aa.mask_self = s->mask_self;
       NB_CUDA(launch_adjoint(aa, a.num_tiles, s->per_pair_mass, s->stream));
-      NB_CUDA(launch_adjoint_finish_v(a.mu, a.lam_v, s->params.damping, s->n_pad, s->stream));
       std::swap(a.lam_x, a.tmp);
+      std::swap(a.lam_v, a.mu);
     }
   }
   NB_CUDA(launch_pack_vec3(a.lam_x, n, s->map_d, stage, s->stream));

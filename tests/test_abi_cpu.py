@@ -220,3 +220,32 @@ def test_plan_work_covers_every_tile_once(sizes, cfg, grid):
     assert sum(len(v) for v in parts.values()) == slots
     for v in parts.values():
         assert [p for _, p in sorted(v)] == list(range(len(v)))
+
+
+def test_null_handles_are_rejected_without_touching_the_device():
+    import ctypes as C
+
+    h = None
+    L = nb.lib
+    one = [(L.nb_sim_step, (h,)), (L.nb_sim_advance, (h, 1)),
+           (L.nb_sim_advance_per_system, (h, 1)), (L.nb_sim_synchronize, (h,)),
+           (L.nb_sim_inject_wait_timeout, (h,)), (L.nb_sim_generate, (h, 1, 1)),
+           (L.nb_sim_get_state, (h,) + (None,) * 6), (L.nb_sim_set_state, (h,) + (None,) * 7),
+           (L.nb_sim_accelerations, (h, None, None, None)),
+           (L.nb_sim_set_stream, (h, None)), (L.nb_sim_export_device, (h, None, None)),
+           (L.nb_sim_set_kernel_config, (h, 0)), (L.nb_sim_autotune, (h, None)),
+           (L.nb_sim_graph_capture, (h, 1)), (L.nb_sim_graph_launch, (h,)),
+           (L.nb_sim_diagnostics, (h, -1, None)),
+           (L.nb_sim_fp64_accelerations, (h, None, 1, None, None, None)),
+           (L.nb_sim_adjoint_forward, (h, 1, 1)),
+           (L.nb_sim_adjoint_backward, (h, None, None, None, None)),
+           (L.nb_sim_render, (h, None, None, 64, 64, None)),
+           (L.nb_sim_time_iterations, (h, 1, 0, None))]
+    for fn, args in one:
+        assert fn(*args) == nb.NB_ERR_INVALID_ARGUMENT, fn.__name__
+    out = C.c_uint64()
+    assert L.nb_sim_num_particles(None, C.byref(out)) == nb.NB_ERR_INVALID_ARGUMENT
+    assert L.nb_sim_destroy(None) == nb.NB_OK          # like free(NULL)
+    assert L.nb_accelerations_noalloc(None, 1, 1.0, 1e-3, None, None) == \
+        nb.NB_ERR_INVALID_ARGUMENT
+    assert "NULL" in L.nb_last_error().decode()
