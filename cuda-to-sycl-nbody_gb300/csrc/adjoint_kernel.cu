@@ -227,6 +227,14 @@ int grid_for(int64_t n) {
 
 int adjoint_tile() { return kAdjBI; }
 
+cudaError_t adjoint_blocks_per_sm(bool per_pair_mass, int* blocks) {
+  return per_pair_mass
+             ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, adjoint_partial_kernel<true>,
+                                                             kAdjThreads, 0)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, adjoint_partial_kernel<false>,
+                                                             kAdjThreads, 0);
+}
+
 cudaError_t launch_adjoint(const AdjointArgs& a, int32_t num_tiles, bool per_pair_mass,
                            cudaStream_t stream) {
   const dim3 grid(num_tiles, a.num_splits);

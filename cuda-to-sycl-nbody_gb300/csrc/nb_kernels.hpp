@@ -70,6 +70,7 @@ struct AdjointArgs {
 cudaError_t launch_adjoint(const AdjointArgs& a, int32_t num_tiles, bool per_pair_mass,
                            cudaStream_t stream);
 int adjoint_tile();  // i-particles per adjoint CTA
+cudaError_t adjoint_blocks_per_sm(bool per_pair_mass, int* blocks);
 // n x 3 interleaved (user order) <-> padded float4.
 cudaError_t launch_unpack_vec3(const float* in, int64_t n, const int64_t* map, float4* out,
                                cudaStream_t stream);

@@ -72,8 +72,11 @@ int ensure_adjoint_buffers(nb_sim* s, int32_t ncp, int32_t every) {
         ti.push_back(t);
       }
     a.num_tiles = static_cast<int32_t>(ts.size());
-    // j-chunks per i-tile: about 8 CTAs per SM in total, deterministic reduction after.
-    const int32_t target = 8 * s->sms;
+    // j-chunks per i-tile: one full wave of resident CTAs (i-tiles x chunks = SMs x
+    // resident CTAs per SM, rounded up), the chunk sums reduced in order afterwards.
+    int per_sm = 1;
+    if (adjoint_blocks_per_sm(s->per_pair_mass, &per_sm) != cudaSuccess || per_sm < 1) per_sm = 1;
+    const int32_t target = per_sm * s->sms;
     a.num_splits = std::max(1, std::min(64, (target + a.num_tiles - 1) / a.num_tiles));
     NB_TRY(dev_alloc(&a.partial, static_cast<size_t>(a.num_splits) * np));
     NB_TRY(dev_alloc(&a.tile_sys, ts.size()));
