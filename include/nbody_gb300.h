@@ -267,7 +267,7 @@ int nb_camera_matrices(float azimuth, float elevation, float distance, const flo
  * 16 x 16 flare texture (genFlareTex, gen.cpp:36-51). */
 int nb_render_tables(float* gauss_offsets, float* gauss_weights, int32_t* taps, float* flare);
 /* Render the current state as the reference's OpenGL renderer does
- * (RendererGL::render, renderer_gl.cpp:96-157; shaders/gl/*): additive
+ * (RendererGL::render, renderer_gl.cpp:96-157, and the shaders in shaders/gl): additive
  * velocity-coloured flare sprites into an HDR buffer with a 50-pixel margin,
  * half-resolution separable Gaussian bloom, mean luminance, exposure tonemap and
  * gamma 2.2 -- on the GPU, with no graphics API.  Writes width x height float4
