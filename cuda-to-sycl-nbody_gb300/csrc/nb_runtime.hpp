@@ -53,6 +53,7 @@ struct AdjointState {
 
 struct nb_sim {
   nb_params params{};
+  int device = 0;  // the CUDA device current when the simulation was created
   int sms = 0;
   std::string device_name;
   cudaStream_t stream = nullptr;
@@ -103,7 +104,28 @@ namespace nbg {
 extern thread_local std::string t_last_error;
 int set_error(int code, const std::string& msg);
 int cuda_error(cudaError_t e, const char* what);
-int check_device(int* sms, cudaDeviceProp* prop);
+// Properties of the current device; NB_ERR_NO_DEVICE unless it is an sm_103 GPU.
+int check_device(int* sms, cudaDeviceProp* prop, int* device = nullptr);
+
+// Makes `dev` current for the lifetime of the guard and restores the caller's
+// device afterwards, so that a simulation always runs on the device it was created
+// on whatever device the calling thread has selected since.
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev_) == cudaSuccess && prev_ != dev && cudaSetDevice(dev) == cudaSuccess)
+      switched_ = true;
+  }
+  ~DeviceGuard() {
+    if (switched_) cudaSetDevice(prev_);
+  }
+  DeviceGuard(const DeviceGuard&) = delete;
+  DeviceGuard& operator=(const DeviceGuard&) = delete;
+
+ private:
+  int prev_ = 0;
+  bool switched_ = false;
+};
 void free_worklist(WorkListDev& w);
 // Free the diagnostics and adjoint buffers of a simulation.
 void release_aux(nb_sim* s);

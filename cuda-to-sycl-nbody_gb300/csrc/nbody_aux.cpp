@@ -95,6 +95,7 @@ extern "C" {
 
 int nb_sim_diagnostics(nb_sim* s, int32_t system, nb_diagnostics* out) {
   if (!s || !out) return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard dg_(s->device);
   const int32_t nsys = static_cast<int32_t>(s->sys_h.size());
   if (system < -1 || system >= nsys) return set_error(NB_ERR_INVALID_ARGUMENT, "bad system");
   if (!s->diag_out_d) NB_TRY(dev_alloc(&s->diag_out_d, 10));
@@ -123,6 +124,7 @@ int nb_sim_fp64_accelerations(nb_sim* s, const uint64_t* rows, uint64_t count, d
                               double* ay, double* az) {
   if (!s || (count && (!rows || !ax || !ay || !az)))
     return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard dg_(s->device);
   if (count == 0) return NB_OK;
   if (count > (1u << 24)) return set_error(NB_ERR_INVALID_ARGUMENT, "too many rows");
   std::vector<int64_t> g(count);
@@ -171,6 +173,7 @@ int nb_sim_fp64_accelerations(nb_sim* s, const uint64_t* rows, uint64_t count, d
 
 int nb_sim_adjoint_forward(nb_sim* s, int32_t T, int32_t checkpoint_every) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   if (T < 1 || checkpoint_every < 1)
     return set_error(NB_ERR_INVALID_ARGUMENT, "T and checkpoint_every must be >= 1");
   if (s->params.calc_method != NB_BRANCH)
@@ -198,6 +201,7 @@ int nb_sim_adjoint_forward(nb_sim* s, int32_t T, int32_t checkpoint_every) {
 int nb_sim_adjoint_backward(nb_sim* s, const float* gx_T, const float* gv_T, float* gx_0,
                             float* gv_0) {
   if (!s || !gx_T || !gx_0 || !gv_0) return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard dg_(s->device);
   AdjointState& a = s->adj;
   if (!a.valid) return set_error(NB_ERR_STATE, "call nb_sim_adjoint_forward first");
   NB_TRY(ensure_staging(s));

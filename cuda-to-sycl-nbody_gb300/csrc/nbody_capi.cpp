@@ -40,7 +40,7 @@ int cuda_error(cudaError_t e, const char* what) {
   return set_error(code, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-int check_device(int* sms, cudaDeviceProp* out_prop) {
+int check_device(int* sms, cudaDeviceProp* out_prop, int* device) {
   int count = 0;
   cudaError_t e = cudaGetDeviceCount(&count);
   if (e != cudaSuccess || count == 0) {
@@ -49,11 +49,16 @@ int check_device(int* sms, cudaDeviceProp* out_prop) {
                                            (e == cudaSuccess ? "device count is 0"
                                                              : cudaGetErrorString(e)));
   }
+  int dev = 0;
+  e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
   cudaDeviceProp prop;
-  e = cudaGetDeviceProperties(&prop, 0);
+  e = cudaGetDeviceProperties(&prop, dev);
   if (e != cudaSuccess) return cuda_error(e, "cudaGetDeviceProperties");
+  if (device) *device = dev;
   if (prop.major != 10 || prop.minor != 3)
-    return set_error(NB_ERR_NO_DEVICE, std::string("device 0 (") + prop.name + ") is sm_" +
+    return set_error(NB_ERR_NO_DEVICE, std::string("device ") + std::to_string(dev) + " (" +
+                                           prop.name + ") is sm_" +
                                            std::to_string(prop.major) +
                                            std::to_string(prop.minor) +
                                            "; this library is built for sm_103a only");
@@ -328,14 +333,14 @@ static int create_impl(const nb_params* p, uint32_t num_systems, const uint32_t*
     return set_error(NB_ERR_INVALID_ARGUMENT,
                      "num_particles (" + std::to_string(p->num_particles) +
                          ") differs from the sum of system sizes (" + std::to_string(total) + ")");
-  int sms = 0;
+  int sms = 0, device = 0;
   cudaDeviceProp prop;
-  NB_TRY(check_device(&sms, &prop));
-  NB_CUDA(cudaSetDevice(0));
+  NB_TRY(check_device(&sms, &prop, &device));
 
   nb_sim* s = new (std::nothrow) nb_sim();
   if (!s) return set_error(NB_ERR_OUT_OF_MEMORY, "host allocation failed");
   s->params = *p;
+  s->device = device;
   s->sms = sms;
   s->device_name = prop.name;
   s->n_real = total;
@@ -482,7 +487,9 @@ int nb_device_name(char* buf, size_t len) {
     std::snprintf(buf, len, "%s", "Unknown Device");
     return set_error(NB_ERR_NO_DEVICE, "no CUDA device");
   }
-  NB_CUDA(cudaGetDeviceProperties(&prop, 0));
+  int dev = 0;
+  NB_CUDA(cudaGetDevice(&dev));
+  NB_CUDA(cudaGetDeviceProperties(&prop, dev));
   std::snprintf(buf, len, "%s", prop.name);
   return NB_OK;
 }
@@ -492,8 +499,9 @@ int nb_device_fp32_peak_tflops(double* tflops) {
   int sms = 0;
   cudaDeviceProp prop;
   NB_TRY(check_device(&sms, &prop));
-  int clock_khz = 0;
-  NB_CUDA(cudaDeviceGetAttribute(&clock_khz, cudaDevAttrClockRate, 0));
+  int clock_khz = 0, dev = 0;
+  NB_CUDA(cudaGetDevice(&dev));
+  NB_CUDA(cudaDeviceGetAttribute(&clock_khz, cudaDevAttrClockRate, dev));
   *tflops = static_cast<double>(sms) * 128.0 * 2.0 * clock_khz * 1e3 / 1e12;
   return NB_OK;
 }
@@ -527,6 +535,7 @@ int nb_ensemble_create(const nb_params* p, uint32_t num_systems, const uint32_t*
 
 int nb_sim_destroy(nb_sim* s) {
   if (!s) return NB_OK;
+  DeviceGuard dg_(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
   for (int b = 0; b < 2; ++b) {
     if (s->gexec[b]) cudaGraphExecDestroy(s->gexec[b]);
@@ -555,6 +564,7 @@ int nb_sim_destroy(nb_sim* s) {
 
 int nb_sim_advance(nb_sim* s, int32_t iterations) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   if (iterations < 0) return set_error(NB_ERR_INVALID_ARGUMENT, "iterations < 0");
   for (int32_t k = 0; k < iterations; ++k) NB_TRY(force_pass(s, nullptr, false));
   return NB_OK;
@@ -562,6 +572,7 @@ int nb_sim_advance(nb_sim* s, int32_t iterations) {
 
 int nb_sim_advance_per_system(nb_sim* s, int32_t iterations) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   if (iterations < 0) return set_error(NB_ERR_INVALID_ARGUMENT, "iterations < 0");
   for (int32_t k = 0; k < iterations; ++k) NB_TRY(force_pass(s, nullptr, true));
   return NB_OK;
@@ -569,12 +580,14 @@ int nb_sim_advance_per_system(nb_sim* s, int32_t iterations) {
 
 int nb_sim_synchronize(nb_sim* s) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   NB_CUDA(cudaStreamSynchronize(s->stream));
   return check_error_word(s);
 }
 
 int nb_sim_time_iterations(nb_sim* s, int32_t iterations, int32_t per_system, float* ms) {
   if (!s || !ms) return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard dg_(s->device);
   if (iterations < 0) return set_error(NB_ERR_INVALID_ARGUMENT, "iterations < 0");
   if (per_system) NB_TRY(build_per_system_worklists(s));
   NB_CUDA(cudaEventRecord(s->ev0, s->stream));
@@ -587,6 +600,7 @@ int nb_sim_time_iterations(nb_sim* s, int32_t iterations, int32_t per_system, fl
 
 int nb_sim_step(nb_sim* s) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   // stepSim (simulator.cu:47-75): the reference times launch-to-sync with a host
   // clock; here the same region is timed with CUDA events on the stream.
   float ms = 0.f;
@@ -597,6 +611,7 @@ int nb_sim_step(nb_sim* s) {
 
 int nb_sim_get_state(nb_sim* s, float* x, float* y, float* z, float* vx, float* vy, float* vz) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   NB_TRY(ensure_staging(s));
   const size_t n = s->n_real;
   NB_CUDA(launch_pack_state(s->pos_d[s->cur], s->vel_d, n, s->map_d, s->staging_d, s->stream));
@@ -612,6 +627,7 @@ int nb_sim_get_state(nb_sim* s, float* x, float* y, float* z, float* vx, float* 
 int nb_sim_set_state(nb_sim* s, const float* x, const float* y, const float* z, const float* vx,
                      const float* vy, const float* vz, const float* mass) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   if (mass) {
     std::vector<float> m(mass, mass + s->n_real);
     assign_mass_mode(s, m);
@@ -630,6 +646,7 @@ int nb_sim_set_state(nb_sim* s, const float* x, const float* y, const float* z, 
 
 int nb_sim_accelerations(nb_sim* s, float* ax, float* ay, float* az) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   NB_TRY(ensure_accel(s));
   NB_TRY(ensure_staging(s));
   NB_TRY(force_pass(s, s->acc_d, false));
@@ -676,6 +693,7 @@ int nb_sim_calc_method(const nb_sim* s, int32_t* method) {
 
 int nb_sim_set_stream(nb_sim* s, void* stream) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   NB_CUDA(cudaStreamSynchronize(s->stream));
   if (s->own_stream) cudaStreamDestroy(s->stream);
   s->own_stream = false;
@@ -685,6 +703,7 @@ int nb_sim_set_stream(nb_sim* s, void* stream) {
 
 int nb_sim_export_device(nb_sim* s, float* pos_xyzm_device, float* vel_xyzw_device) {
   if (!s || !pos_xyzm_device) return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard dg_(s->device);
   if ((reinterpret_cast<uintptr_t>(pos_xyzm_device) & 15) ||
       (reinterpret_cast<uintptr_t>(vel_xyzw_device) & 15))
     return set_error(NB_ERR_INVALID_ARGUMENT, "device buffers must be 16-byte aligned");
@@ -706,6 +725,7 @@ int nb_kernel_config_info(int32_t index, nb_kernel_info* info) {
 
 int nb_sim_set_kernel_config(nb_sim* s, int32_t index) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   if (index < -1 || index >= num_force_configs())
     return set_error(NB_ERR_INVALID_ARGUMENT, "bad config index");
   const int cfg = index < 0 ? default_config(s) : index;
@@ -724,6 +744,7 @@ int nb_sim_kernel_info(const nb_sim* s, nb_kernel_info* info) {
 
 int nb_sim_autotune(nb_sim* s, int32_t* chosen) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   NB_TRY(ensure_accel(s));
   int best = s->cfg;
   float best_ms = 1e30f;
@@ -795,6 +816,7 @@ int nb_plan_work(uint32_t num_systems, const uint32_t* sizes, int32_t config_ind
 
 int nb_sim_generate(nb_sim* s, int32_t kind, uint64_t seed) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   if (kind != NB_IC_THIN_DISK && kind != NB_IC_PLUMMER && kind != NB_IC_TWO_DISKS)
     return set_error(NB_ERR_INVALID_ARGUMENT, "unknown initial-condition kind");
   const int32_t nsys = static_cast<int32_t>(s->sys_h.size());
@@ -838,6 +860,7 @@ int nb_sim_generate(nb_sim* s, int32_t kind, uint64_t seed) {
 
 int nb_sim_inject_wait_timeout(nb_sim* s) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   if (s->params.calc_method != NB_BRANCH)
     return set_error(NB_ERR_STATE, "the PREDICATED kernel has no device-side waits");
   s->inject_timeout = 1;
@@ -846,6 +869,7 @@ int nb_sim_inject_wait_timeout(nb_sim* s) {
 
 int nb_sim_graph_capture(nb_sim* s, int32_t iterations) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   if (iterations <= 0) return set_error(NB_ERR_INVALID_ARGUMENT, "iterations must be > 0");
   if (s->stream == nullptr)
     return set_error(NB_ERR_STATE, "graph capture needs a non-default stream");
@@ -886,6 +910,7 @@ int nb_sim_graph_capture(nb_sim* s, int32_t iterations) {
 
 int nb_sim_graph_launch(nb_sim* s) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
   if (!s->gexec[s->cur]) return set_error(NB_ERR_STATE, "no graph captured");
   NB_CUDA(cudaGraphLaunch(s->gexec[s->cur], s->stream));
   s->cur ^= (s->graph_iters & 1);

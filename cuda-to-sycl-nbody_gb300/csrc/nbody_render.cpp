@@ -150,6 +150,7 @@ int nb_sim_render(nb_sim* s, const float view[16], const float proj[16], int32_t
                   int32_t height, float* rgba_device) {
   if (!s || !view || !proj || !rgba_device)
     return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard dg_(s->device);
   if (width < 16 || height < 16 || width > 16384 || height > 16384)
     return set_error(NB_ERR_INVALID_ARGUMENT, "image size must be in [16, 16384]");
   if (reinterpret_cast<uintptr_t>(rgba_device) & 15)
