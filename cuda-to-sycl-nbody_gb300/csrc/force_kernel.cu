@@ -10,18 +10,21 @@ extern const ConfigEntry kForceShapesA[];
 extern const int kNumForceShapesA;
 extern const ConfigEntry kForceShapesB[];
 extern const int kNumForceShapesB;
+extern const ConfigEntry kForceShapesC[];
+extern const int kNumForceShapesC;
 
 namespace {
 
 const ConfigEntry& entry(int index) {
   if (index < kNumForceShapesA) return kForceShapesA[index];
   index -= kNumForceShapesA;
-  return kForceShapesB[index];
+  if (index < kNumForceShapesB) return kForceShapesB[index];
+  return kForceShapesC[index - kNumForceShapesB];
 }
 
 }  // namespace
 
-int num_force_configs() { return kNumForceShapesA + kNumForceShapesB; }
+int num_force_configs() { return kNumForceShapesA + kNumForceShapesB + kNumForceShapesC; }
 
 KernelShape force_config_shape(int index) { return entry(index).shape; }
 

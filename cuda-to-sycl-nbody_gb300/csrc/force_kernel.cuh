@@ -395,9 +395,23 @@ __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
   }
 }
 
+// Shapes whose tile ring needs 48 KB or more of dynamic shared memory opt in to it
+// once per process (with the kernel's static shared memory the 48 KB default is
+// exceeded at exactly 48 KB).
+template <int T, int R, int BJ, int S, int U, bool C, bool M>
+cudaError_t smem_opt_in() {
+  constexpr int smem = S * BJ * 16;
+  if (smem < 48 * 1024) return cudaSuccess;
+  static cudaError_t status = cudaFuncSetAttribute(
+      force_kernel<T, R, BJ, S, U, C, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  return status;
+}
+
 template <int T, int R, int BJ, int S, int U, bool C, bool M>
 cudaError_t launch_one(const ForceArgs& a, int grid, cudaStream_t st) {
   constexpr int smem = S * BJ * 16;
+  const cudaError_t e = smem_opt_in<T, R, BJ, S, U, C, M>();
+  if (e != cudaSuccess) return e;
   force_kernel<T, R, BJ, S, U, C, M><<<grid, T, smem, st>>>(a);
   return cudaGetLastError();
 }
@@ -405,6 +419,8 @@ cudaError_t launch_one(const ForceArgs& a, int grid, cudaStream_t st) {
 template <int T, int R, int BJ, int S, int U, bool C, bool M>
 cudaError_t occ_one(int* blocks) {
   constexpr int smem = S * BJ * 16;
+  const cudaError_t e = smem_opt_in<T, R, BJ, S, U, C, M>();
+  if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, force_kernel<T, R, BJ, S, U, C, M>,
                                                        T, smem);
 }

@@ -1,5 +1,5 @@
-// Force kernel shapes 0-3.  1 (256 x 4, one CTA per SM) is the default for large systems, 3 for
-// ensembles of small systems; 0 is the shape of nb_accelerations_noalloc.
+// Force kernel shapes 0-3.  3 is the default for ensembles of small systems; 0 is the
+// shape of nb_accelerations_noalloc.
 #include "force_kernel.cuh"
 
 namespace nbg {

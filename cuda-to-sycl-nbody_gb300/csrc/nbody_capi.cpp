@@ -302,15 +302,15 @@ int check_error_word(nb_sim* s) {
 }
 
 static int default_config(const nb_sim* s) {
-  // Large systems: 256 x 4 (1024-particle i-tiles, one CTA per SM); ensembles of
-  // small systems: 256 x 2.
+  // Large systems: 256 x 4 with 2048-particle j-tiles (one CTA per SM); ensembles of
+  // small systems: 256 x 2 with 256-particle j-tiles.
   int64_t sum_n2 = 0, sum_n3 = 0;
   for (const auto& d : s->sys_h) {
     sum_n2 += static_cast<int64_t>(d.n) * d.n;
     sum_n3 += static_cast<int64_t>(d.n) * d.n / 64 * d.n / 64;
   }
   const double weighted_n = sum_n2 ? static_cast<double>(sum_n3) * 4096.0 / sum_n2 : 0.0;
-  return weighted_n >= 16384.0 ? 1 : 3;
+  return weighted_n >= 16384.0 ? 9 : 3;
 }
 
 static int create_impl(const nb_params* p, uint32_t num_systems, const uint32_t* sizes, const float* x,
