@@ -197,6 +197,10 @@ __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
   constexpr int BI = THREADS * R;
   constexpr int TILE_BYTES = BJ * 16;
   static_assert(BJ % kPadQuantum == 0, "tile must hold whole padding quanta");
+  // Every tile (a full one or a system's last, partial one) holds a multiple of
+  // kPadQuantum / 2 j-pairs; the pair loop steps U pairs at a time without a
+  // remainder, so U must divide that count or the last step reads past the tile.
+  static_assert((kPadQuantum / 2) % U == 0, "U must divide the j-pairs of a padding quantum");
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   __shared__ int s_last;
