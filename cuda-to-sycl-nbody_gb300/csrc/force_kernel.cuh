@@ -36,6 +36,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 
 #include "nb_device.cuh"
@@ -400,15 +401,23 @@ __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
 }
 
 // Shapes whose tile ring needs 48 KB or more of dynamic shared memory opt in to it
-// once per process (with the kernel's static shared memory the 48 KB default is
-// exceeded at exactly 48 KB).
+// (with the kernel's static shared memory the 48 KB default is exceeded at exactly
+// 48 KB). The attribute belongs to the kernel's instance on the current device, so
+// the opt-in is made once per device ordinal (ordinals >= 64 opt in on every call).
 template <int T, int R, int BJ, int S, int U, bool C, bool M>
 cudaError_t smem_opt_in() {
   constexpr int smem = S * BJ * 16;
   if (smem < 48 * 1024) return cudaSuccess;
-  static cudaError_t status = cudaFuncSetAttribute(
-      force_kernel<T, R, BJ, S, U, C, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  return status;
+  static std::atomic<uint64_t> opted{0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const uint64_t bit = dev >= 0 && dev < 64 ? uint64_t{1} << dev : 0;
+  if (bit != 0 && (opted.load(std::memory_order_acquire) & bit) != 0) return cudaSuccess;
+  e = cudaFuncSetAttribute(force_kernel<T, R, BJ, S, U, C, M>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess && bit != 0) opted.fetch_or(bit, std::memory_order_release);
+  return e;
 }
 
 template <int T, int R, int BJ, int S, int U, bool C, bool M>
