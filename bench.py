@@ -216,9 +216,10 @@ def run_ours(args, rank, world) -> dict:
     flush = torch.empty(max(1, args.flush_mib) << 20, dtype=torch.uint8, device="cuda")
     peak_tf = nb.fp32_peak_tflops()
 
-    # Both accumulators: force error against FP64 at the initial state, then the rate.
+    # Every accumulator: force error against FP64 at the initial state, then the rate.
     modes = {}
-    for name, acc in (("plain", nb.ACC_PLAIN), ("compensated", nb.ACC_COMPENSATED)):
+    for name, acc in (("plain", nb.ACC_PLAIN), ("compensated", nb.ACC_COMPENSATED),
+                      ("reference_order", nb.ACC_REFERENCE_ORDER)):
         if args.acc != "auto" and args.acc != name:
             continue
         p = nb.SimParam(numParticles=n, G=1.0, dt=DT, damping=1.0, distEps=EPS2, accumulator=acc)
@@ -598,9 +599,12 @@ def main() -> int:
                     help="L2 flush buffer written between timed steps (0: no flush; profiling)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
-    ap.add_argument("--acc", choices=["auto", "plain", "compensated"], default="auto",
-                    help="accumulator(s) to measure; auto: both, headline = the faster of those "
-                         "whose force error vs FP64 is <= 1e-5 relative RMS")
+    ap.add_argument("--acc", choices=["auto", "plain", "compensated", "reference_order"],
+                    default="auto",
+                    help="accumulator(s) to measure; auto: all three, headline = the fastest of "
+                         "those whose force error vs FP64 is <= 1e-5 relative RMS "
+                         "(reference_order: the reference's own summation, bit-identical to "
+                         "its kernel)")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the FP64 force-error check (profiling runs)")
     args = ap.parse_args()

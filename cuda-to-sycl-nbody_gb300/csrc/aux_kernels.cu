@@ -36,7 +36,7 @@ __global__ void predicated_kernel(const ForceArgs a, const SystemDesc sd) {
     const float rx = a.pos[pair_index(gj, 0)] - xi;
     const float ry = a.pos[pair_index(gj, 1)] - yi;
     const float rz = a.pos[pair_index(gj, 2)] - zi;
-    const float d2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx)) + a.eps2;
+    const float d2 = fmaf(rz, rz, fmaf(rx, rx, ry * ry)) + a.eps2;
     float inv = rsqrtf(d2 * d2 * d2);
     if (!sd.equal_mass) inv *= a.pos[pair_index(gj, 3)];
     const float mask = (j == li) ? 1.f : 0.f;

@@ -22,6 +22,16 @@ cudaError_t force_blocks_per_sm(int index, bool compensated, bool per_pair_mass,
 cudaError_t launch_predicated(const ForceArgs& a, const SystemDesc& sd, int32_t sys_index,
                               cudaStream_t stream);
 
+// ---- reference-order force + integrate (reference_order_kernel.cu) -------------------
+// particle_interaction<BRANCH> with the reference's per-particle summation order
+// and arithmetic (bit-identical results on the same GPU), equal masses per system.
+// `tiles` holds (system, i-tile) pairs of reference_order_tile() i-particles.
+int reference_order_tile();
+KernelShape reference_order_shape();  // threads, i-particles per thread, j-tile, 2 buffers
+cudaError_t reference_order_blocks_per_sm(int* blocks);
+cudaError_t launch_reference_order(const ForceArgs& a, const int32_t* tiles, int32_t num_tiles,
+                                   int grid, cudaStream_t stream);
+
 // ---- state movement (aux_kernels.cu) ------------------------------------------------
 // Device SoA staging <-> simulation layout.  `map` holds, for each of the n real
 // particles in user order, its padded device index.

@@ -85,6 +85,12 @@ struct nb_sim {
   int32_t* counters_d = nullptr;
   size_t counters_cap = 0;
 
+  // NB_ACC_REFERENCE_ORDER: (system, i-tile) pairs of the reference-order kernel,
+  // the first tile of each system (systems + 1 entries) and its grid.
+  int32_t* ro_tiles_d = nullptr;
+  std::vector<int32_t> ro_first;
+  int ro_grid = 0;
+
   cudaEvent_t ev0 = nullptr;
   cudaEvent_t ev1 = nullptr;
   float last_ms = 0.f;

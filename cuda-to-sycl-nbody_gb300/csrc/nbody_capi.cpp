@@ -85,9 +85,11 @@ static int validate_params(const nb_params* p) {
   if (p->dist_eps < 0.f) return set_error(NB_ERR_INVALID_ARGUMENT, "dist_eps must be >= 0");
   if (p->calc_method != NB_BRANCH && p->calc_method != NB_PREDICATED)
     return set_error(NB_ERR_INVALID_ARGUMENT, "calc_method must be NB_BRANCH or NB_PREDICATED");
-  if (p->accumulator != NB_ACC_PLAIN && p->accumulator != NB_ACC_COMPENSATED)
+  if (p->accumulator != NB_ACC_PLAIN && p->accumulator != NB_ACC_COMPENSATED &&
+      p->accumulator != NB_ACC_REFERENCE_ORDER)
     return set_error(NB_ERR_INVALID_ARGUMENT,
-                     "accumulator must be NB_ACC_PLAIN or NB_ACC_COMPENSATED");
+                     "accumulator must be NB_ACC_PLAIN, NB_ACC_COMPENSATED or "
+                     "NB_ACC_REFERENCE_ORDER");
   if (p->iters_per_frame < 0) return set_error(NB_ERR_INVALID_ARGUMENT, "iters_per_frame < 0");
   return NB_OK;
 }
@@ -237,6 +239,39 @@ static int build_per_system_worklists(nb_sim* s) {
   return NB_OK;
 }
 
+// Tile table of the reference-order kernel (built once, at creation: the
+// systems never change afterwards).
+static int build_reference_order_tiles(nb_sim* s) {
+  const int bi = reference_order_tile();
+  std::vector<int32_t> t;
+  s->ro_first.assign(1, 0);
+  for (int32_t k = 0; k < static_cast<int32_t>(s->sys_h.size()); ++k) {
+    const int32_t count = (s->sys_h[k].n + bi - 1) / bi;
+    for (int32_t it = 0; it < count; ++it) {
+      t.push_back(k);
+      t.push_back(it);
+    }
+    s->ro_first.push_back(s->ro_first.back() + count);
+  }
+  NB_TRY(dev_alloc(&s->ro_tiles_d, t.size()));
+  NB_CUDA(cudaMemcpyAsync(s->ro_tiles_d, t.data(), t.size() * sizeof(int32_t),
+                          cudaMemcpyHostToDevice, s->stream));
+  NB_CUDA(cudaStreamSynchronize(s->stream));  // the host vector dies on return
+  int blocks = 0;
+  if (reference_order_blocks_per_sm(&blocks) != cudaSuccess || blocks < 1) blocks = 1;
+  s->ro_grid = blocks * s->sms;
+  return NB_OK;
+}
+
+// Reference-order pass over systems [k0, k1): one launch over their tiles.
+static int launch_reference_order_range(nb_sim* s, const ForceArgs& a, int32_t k0, int32_t k1) {
+  const int32_t first = s->ro_first[k0];
+  const int32_t count = s->ro_first[k1] - first;
+  NB_CUDA(launch_reference_order(a, s->ro_tiles_d + 2 * static_cast<int64_t>(first), count,
+                                 std::min(s->ro_grid, count), s->stream));
+  return NB_OK;
+}
+
 ForceArgs base_args(nb_sim* s) {
   ForceArgs a{};
   a.pos = s->pos_d[s->cur];
@@ -274,6 +309,17 @@ int force_pass(nb_sim* s, float4* accel_out, bool per_system) {
   if (s->params.calc_method == NB_PREDICATED) {
     for (int32_t k = 0; k < static_cast<int32_t>(s->sys_h.size()); ++k)
       NB_CUDA(launch_predicated(a, s->sys_h[k], k, s->stream));
+  } else if (s->params.accumulator == NB_ACC_REFERENCE_ORDER) {
+    if (s->per_pair_mass)
+      return set_error(NB_ERR_INVALID_ARGUMENT,
+                       "NB_ACC_REFERENCE_ORDER needs equal masses within each system (the "
+                       "reference has unit masses)");
+    const int32_t nsys = static_cast<int32_t>(s->sys_h.size());
+    if (per_system) {
+      for (int32_t k = 0; k < nsys; ++k) NB_TRY(launch_reference_order_range(s, a, k, k + 1));
+    } else {
+      NB_TRY(launch_reference_order_range(s, a, 0, nsys));
+    }
   } else if (per_system) {
     NB_TRY(build_per_system_worklists(s));
     for (const auto& w : s->wl_sys) NB_TRY(launch_with(s, a, w));
@@ -405,6 +451,7 @@ static int create_impl(const nb_params* p, uint32_t num_systems, const uint32_t*
     return fail(cuda_error(e, "copy state"));
   s->cfg = default_config(s);
   if ((st = build_main_worklist(s, s->cfg)) != NB_OK) return fail(st);
+  if ((st = build_reference_order_tiles(s)) != NB_OK) return fail(st);
   if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return fail(cuda_error(e, "create"));
   *out = s;
   return NB_OK;
@@ -553,6 +600,7 @@ int nb_sim_destroy(nb_sim* s) {
   dev_free(s->err_d);
   dev_free(s->partials_d);
   dev_free(s->counters_d);
+  dev_free(s->ro_tiles_d);
   release_aux(s);
   release_render_buffers(s);
   if (s->ev0) cudaEventDestroy(s->ev0);
@@ -736,6 +784,13 @@ int nb_sim_set_kernel_config(nb_sim* s, int32_t index) {
 
 int nb_sim_kernel_info(const nb_sim* s, nb_kernel_info* info) {
   if (!s || !info) return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (s->params.accumulator == NB_ACC_REFERENCE_ORDER) {
+    const KernelShape sh = reference_order_shape();
+    const int32_t tiles = s->ro_first.empty() ? 0 : s->ro_first.back();
+    *info = nb_kernel_info{-1, sh.threads, sh.r, sh.bj, sh.stages, std::min(s->ro_grid, tiles),
+                           tiles, 0};
+    return NB_OK;
+  }
   const KernelShape sh = force_config_shape(s->cfg);
   *info = nb_kernel_info{s->cfg, sh.threads, sh.r, sh.bj, sh.stages,
                          s->wl.grid, s->wl.nseg, s->wl.split};
@@ -745,6 +800,11 @@ int nb_sim_kernel_info(const nb_sim* s, nb_kernel_info* info) {
 int nb_sim_autotune(nb_sim* s, int32_t* chosen) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
   DeviceGuard dg_(s->device);
+  if (s->params.calc_method == NB_PREDICATED || s->params.accumulator == NB_ACC_REFERENCE_ORDER) {
+    // These modes run kernels of one fixed shape: nothing to choose.
+    if (chosen) *chosen = s->cfg;
+    return NB_OK;
+  }
   NB_TRY(ensure_accel(s));
   int best = s->cfg;
   float best_ms = 1e30f;

@@ -32,6 +32,7 @@ BRANCH = 0
 PREDICATED = 1
 ACC_PLAIN = 0
 ACC_COMPENSATED = 1
+ACC_REFERENCE_ORDER = 2
 IC_THIN_DISK = 1
 IC_PLUMMER = 2
 IC_TWO_DISKS = 3

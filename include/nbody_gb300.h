@@ -49,9 +49,19 @@ typedef enum nb_status {
  * force is zero except where a pair term is not finite (simulator.cu:208-209). */
 typedef enum nb_calc_method { NB_BRANCH = 0, NB_PREDICATED = 1 } nb_calc_method;
 
-/* Per-particle force accumulator.  COMPENSATED keeps a Kahan-compensated FP32
- * running sum per particle; the pair arithmetic is FP32 in both modes. */
-typedef enum nb_accumulator { NB_ACC_PLAIN = 0, NB_ACC_COMPENSATED = 1 } nb_accumulator;
+/* Per-particle force accumulator; the pair arithmetic is FP32 in every mode.
+ * PLAIN and COMPENSATED run the tuned kernel, which sums each particle's terms in
+ * its own order (COMPENSATED keeps a Kahan-compensated FP32 running sum).
+ * REFERENCE_ORDER sums them the way particle_interaction<BRANCH> does
+ * (simulator.cu:196-207: one FP32 running sum over j in index order, the same
+ * contracted operations), so on the same GPU its results are bit-identical to the
+ * reference kernel's; it needs equal masses within each system (the reference has
+ * unit masses) and does not use the kernel shapes or the autotuner. */
+typedef enum nb_accumulator {
+  NB_ACC_PLAIN = 0,
+  NB_ACC_COMPENSATED = 1,
+  NB_ACC_REFERENCE_ORDER = 2
+} nb_accumulator;
 
 /* Mirror of SimParam (sim_param.hpp:30-39), plus the accumulator mode.
  * `dist_eps` is the softening added to r^2 (the reference's distEps). */
@@ -80,6 +90,8 @@ typedef struct nb_diagnostics {
 } nb_diagnostics;
 
 /* Kernel shape selected for a simulation (see nb_sim_autotune). */
+/* For NB_ACC_REFERENCE_ORDER, config_index is -1 and the fields describe the
+ * reference-order kernel (segments = its i-tiles, no split tiles). */
 typedef struct nb_kernel_info {
   int32_t config_index;
   int32_t threads_per_block;
@@ -197,7 +209,8 @@ int nb_kernel_config_info(int32_t index, nb_kernel_info* info);
 int nb_sim_set_kernel_config(nb_sim* s, int32_t index);
 int nb_sim_kernel_info(const nb_sim* s, nb_kernel_info* info);
 /* Time every kernel shape on this simulation's data (accelerations only, the
- * state is not advanced) and keep the fastest; `chosen` may be NULL. */
+ * state is not advanced) and keep the fastest; `chosen` may be NULL.  A no-op
+ * for NB_PREDICATED and NB_ACC_REFERENCE_ORDER, whose kernels have one shape. */
 int nb_sim_autotune(nb_sim* s, int32_t* chosen);
 
 /* Plan the work list of kernel shape `config_index` for systems of the given

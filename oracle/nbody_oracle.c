@@ -35,8 +35,9 @@ static void force_fp32(int64_t n, const float* x, const float* y, const float* z
     const float rx = x[i] - px; /* other_pos - pos, :199 */
     const float ry = y[i] - py;
     const float rz = z[i] - pz;
-    /* dot(r, r) + distEps (:201), contracted as (r.z*r.z + (r.y*r.y + r.x*r.x)) */
-    const float d2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx)) + eps;
+    /* dot(r, r) + distEps (:201), contracted as nvcc does for the reference:
+     * fma(r.z, r.z, fma(r.x, r.x, r.y * r.y)) + distEps */
+    const float d2 = fmaf(rz, rz, fmaf(rx, rx, ry * ry)) + eps;
     float inv = 1.0f / sqrtf(d2 * d2 * d2); /* rsqrt(d2^3), :202 */
     if (mass) inv *= mass[i];
     if (method == ORACLE_BRANCH) {

@@ -1,0 +1,127 @@
+"""GPU parity of the reference-order accumulator (NB_ACC_REFERENCE_ORDER): bit for
+bit against the reference kernel particle_interaction<BRANCH>
+(src/simulator.cu:186-229) -- its golden fixtures and live runs of the kernel
+itself, built from the reference's source -- on the same inputs.
+
+Tolerance: none.  Every output word (x, y, z, vx, vy, vz) must be identical.
+"""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import nbody_gb300 as nb
+import oracle_binding as orc
+from helpers import disk_case, params, vec_errors
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+BRANCH_CASES = sorted(p.stem for p in GOLDEN.glob("*.npz")
+                      if json.loads(str(np.load(p)["params"]))["method"] == nb.BRANCH)
+needs_reference = pytest.mark.skipif(not orc.reference_available(),
+                                     reason="reference kernel cubin not built")
+
+
+def same_bits(got, ref):
+    return all(np.array_equal(np.asarray(g, np.float32).view(np.uint32),
+                              np.asarray(r, np.float32).view(np.uint32))
+               for g, r in zip(got, ref))
+
+
+def ro_params(n, **kw):
+    return params(n, acc=nb.ACC_REFERENCE_ORDER, **kw)
+
+
+def test_branch_golden_cases_present():
+    assert {"config0_n2048", "force_sum_n1000", "perf_args_n1280", "ragged_n333",
+            "reference_default_n1024"} <= set(BRANCH_CASES)
+
+
+@pytest.mark.parametrize("name", BRANCH_CASES)
+def test_bitwise_equal_to_golden_fixtures(name):
+    d = np.load(GOLDEN / f"{name}.npz")
+    prm = json.loads(str(d["params"]))
+    pos = [d["x"], d["y"], d["z"]]
+    vel = [d["vx"], d["vy"], d["vz"]]
+    out = [d[f"out_{c}"] for c in ("x", "y", "z", "vx", "vy", "vz")]
+    n = pos[0].size
+    p = nb.SimParam(numParticles=n, G=prm["G"], dt=prm["dt"], damping=prm["damping"],
+                    distEps=prm["eps"], calcMethod=nb.BRANCH, accumulator=nb.ACC_REFERENCE_ORDER)
+    with nb.Simulation(p, pos, vel, None) as sim:
+        sim.advance(prm["iters"])
+        got = sim.get_state()
+    assert same_bits(got, out), name
+
+
+@needs_reference
+@pytest.mark.parametrize("n,eps,iters", [(1, 1e-3, 2), (2, 1e-3, 2), (17, 1e-3, 3),
+                                         (333, 0.0, 3), (1000, 1e-3, 5), (4099, 1e-3, 2),
+                                         (25600, 1e-3, 10)])
+def test_bitwise_equal_to_reference_kernel(n, eps, iters):
+    pos, vel, _ = disk_case(n, seed=n + 7, eps=max(eps, 1e-6))
+    ref, _ = orc.reference_run(pos, vel, 1.0, 1e-3, 0.999, eps, iters=iters, method=orc.BRANCH)
+    with nb.Simulation(ro_params(n, eps=eps), pos, vel, None) as sim:
+        sim.advance(iters)
+        got = sim.get_state()
+    assert same_bits(got, ref)
+
+
+@needs_reference
+def test_ensemble_systems_each_equal_to_reference_kernel():
+    sizes = [333, 17, 1000, 2048, 1]
+    rng = np.random.default_rng(5)
+    pos = [rng.uniform(-1, 1, sum(sizes)).astype(np.float32) for _ in range(3)]
+    vel = [rng.uniform(-0.1, 0.1, sum(sizes)).astype(np.float32) for _ in range(3)]
+    p = ro_params(sum(sizes), eps=1e-3)
+    with nb.Simulation(p, pos, vel, None, sizes=sizes) as sim:
+        sim.advance(3)
+        got = sim.get_state()
+    start = 0
+    for n in sizes:
+        sl = slice(start, start + n)
+        ref, _ = orc.reference_run([a[sl] for a in pos], [a[sl] for a in vel], 1.0, 1e-3, 0.999,
+                                   1e-3, iters=3, method=orc.BRANCH)
+        assert same_bits([g[sl] for g in got], ref), n
+        start += n
+
+
+def test_per_system_launches_and_graph_match_one_launch():
+    sizes = [700, 64, 1500]
+    rng = np.random.default_rng(9)
+    pos = [rng.uniform(-1, 1, sum(sizes)).astype(np.float32) for _ in range(3)]
+    vel = [np.zeros(sum(sizes), np.float32) for _ in range(3)]
+    p = ro_params(sum(sizes))
+    outs = []
+    for how in ("advance", "per_system", "graph"):
+        with nb.Simulation(p, pos, vel, None, sizes=sizes) as sim:
+            if how == "advance":
+                sim.advance(4)
+            elif how == "per_system":
+                sim.advance_per_system(4)
+            else:
+                sim.graph_capture(4)
+                sim.graph_launch()
+            outs.append(sim.get_state())
+    assert same_bits(outs[1], outs[0]) and same_bits(outs[2], outs[0])
+
+
+def test_accelerations_agree_with_oracle():
+    n = 3000
+    pos, vel, m = disk_case(n, seed=3)
+    with nb.Simulation(ro_params(n), pos, vel, None) as sim:
+        got = sim.accelerations()
+    rms, mx = vec_errors(got, orc.accel_fp32(pos, None, 1.0, 1e-3))
+    assert rms <= 1e-5 and mx <= 1e-4
+
+
+def test_unequal_masses_are_rejected():
+    n = 64
+    pos, vel, _ = disk_case(n, seed=4)
+    m = np.linspace(1.0, 2.0, n).astype(np.float32)
+    with nb.Simulation(ro_params(n), pos, vel, m) as sim:
+        with pytest.raises(nb.NbError) as e:
+            sim.advance(1)
+    assert e.value.status == nb.NB_ERR_INVALID_ARGUMENT
