@@ -29,7 +29,7 @@ namespace nbg {
 namespace {
 
 constexpr int kRoThreads = 128;  // threads per CTA
-constexpr int kRoPairs = 2;      // i-pairs per thread (4 i-particles)
+constexpr int kRoPairs = 4;      // i-pairs per thread (8 i-particles)
 constexpr int kRoBI = kRoThreads * 2 * kRoPairs;  // i-particles per tile
 constexpr int kRoBJ = 256;       // j-particles per shared-memory tile
 constexpr int kRoRecs = kRoBJ / 2;                // 32-byte pair records per j-tile
