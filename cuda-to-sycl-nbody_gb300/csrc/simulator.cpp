@@ -25,6 +25,7 @@ SimParam::SimParam() {
   distEps = p.dist_eps;
   gwSize = p.gw_size;
   calcMethod = CalculationMethod::BRANCH;
+  accumulator = p.accumulator;
 }
 
 void SimParam::parseArgs(int argc, char** argv) {
@@ -57,6 +58,7 @@ nb_params SimParam::toC() const {
   p.dist_eps = distEps;
   p.gw_size = gwSize;
   p.calc_method = calcMethod == CalculationMethod::PREDICATED ? NB_PREDICATED : NB_BRANCH;
+  p.accumulator = accumulator;
   return p;
 }
 

@@ -36,6 +36,9 @@ class SimParam {
   float distEps;
   int gwSize;
   CalculationMethod calcMethod;
+  // Not in the reference: how each particle's force is summed (nb_accumulator;
+  // NB_ACC_REFERENCE_ORDER reproduces the reference kernel bit for bit).
+  int accumulator;
 
   nb_params toC() const;
 };

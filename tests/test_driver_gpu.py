@@ -32,3 +32,41 @@ def test_driver_rejects_unknown_method():
                        capture_output=True, text=True, timeout=60)
     assert r.returncode == 1
     assert "BRANCH or PREDICATED" in r.stderr
+
+
+def test_driver_reference_order_state_is_the_reference_kernels(tmp_path):
+    """Same argv as the reference's binary, reference-order accumulation: the final
+    state equals the reference kernel's, run from the same initial disk
+    (DiskGalaxySimulator's generator, simulator.cu:131-158), word for word."""
+    import os
+
+    import numpy as np
+
+    import oracle_binding as orc
+
+    if not orc.reference_available():
+        pytest.skip("reference kernel cubin not built")
+    batches, iters, frames = 4, 2, 6
+    out = tmp_path / "state.f32"
+    env = dict(os.environ, NBODY_GB300_ACCUMULATOR="reference_order",
+               NBODY_GB300_STATE_OUT=str(out))
+    r = subprocess.run([str(nb.DRIVER_PATH), str(batches), str(iters), "0.999", "0.001", "1.0e-3",
+                        "2.0", str(frames)], capture_output=True, text=True, timeout=120, env=env)
+    assert r.returncode == 0, r.stderr
+    n = 256 * batches
+    got = np.fromfile(out, dtype=np.float32).reshape(6, n)
+    pos, vel = nb.reference_disk(n)
+    ref, _ = orc.reference_run(pos, vel, 2.0, 0.001, 0.999, 1.0e-3, iters=iters * frames,
+                               method=orc.BRANCH)
+    assert all(np.array_equal(g.view(np.uint32), np.asarray(x, np.float32).view(np.uint32))
+               for g, x in zip(got, ref))
+
+
+def test_driver_rejects_unknown_accumulator():
+    import os
+
+    env = dict(os.environ, NBODY_GB300_ACCUMULATOR="kahan")
+    r = subprocess.run([str(nb.DRIVER_PATH), "1", "1"], capture_output=True, text=True, timeout=60,
+                       env=env)
+    assert r.returncode == 1
+    assert "reference_order" in r.stderr
