@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -108,6 +110,9 @@ struct nb_sim {
 namespace nbg {
 
 extern thread_local std::string t_last_error;
+// Failure-detection hook (nb_inject_alloc_failure): while positive, each device
+// allocation counts it down, and the one that brings it to zero fails.
+extern std::atomic<int> g_alloc_failure_countdown;
 int set_error(int code, const std::string& msg);
 int cuda_error(cudaError_t e, const char* what);
 // Properties of the current device; NB_ERR_NO_DEVICE unless it is an sm_103 GPU.
@@ -141,6 +146,9 @@ template <class T>
 int dev_alloc(T** p, size_t count) {
   *p = nullptr;
   if (count == 0) return NB_OK;
+  if (g_alloc_failure_countdown.load(std::memory_order_relaxed) > 0 &&
+      g_alloc_failure_countdown.fetch_sub(1) == 1)
+    return set_error(NB_ERR_OUT_OF_MEMORY, "injected allocation failure (nb_inject_alloc_failure)");
   const cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
   if (e != cudaSuccess) {
     *p = nullptr;

@@ -29,6 +29,7 @@ using namespace nbg;
 namespace nbg {
 
 thread_local std::string t_last_error;
+std::atomic<int> g_alloc_failure_countdown{0};
 
 int set_error(int code, const std::string& msg) {
   t_last_error = msg;
@@ -623,6 +624,12 @@ int nb_sim_advance_per_system(nb_sim* s, int32_t iterations) {
   DeviceGuard dg_(s->device);
   if (iterations < 0) return set_error(NB_ERR_INVALID_ARGUMENT, "iterations < 0");
   for (int32_t k = 0; k < iterations; ++k) NB_TRY(force_pass(s, nullptr, true));
+  return NB_OK;
+}
+
+int nb_inject_alloc_failure(int32_t nth) {
+  if (nth < 0) return set_error(NB_ERR_INVALID_ARGUMENT, "nth must be >= 0");
+  g_alloc_failure_countdown.store(nth);
   return NB_OK;
 }
 

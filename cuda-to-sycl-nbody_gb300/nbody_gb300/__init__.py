@@ -128,6 +128,7 @@ SIGNATURES = {
     "nb_sim_autotune": (C.c_int, [_P, _I32]),
     "nb_plan_work": (C.c_int, [C.c_uint32, _U32, C.c_int32, C.c_int32, C.POINTER(nb_segment),
                                C.c_int32, _I32, _I32, _I32, _I32, _I32]),
+    "nb_inject_alloc_failure": (C.c_int, [C.c_int32]),
     "nb_sim_graph_capture": (C.c_int, [_P, C.c_int32]),
     "nb_sim_graph_launch": (C.c_int, [_P]),
     "nb_sim_diagnostics": (C.c_int, [_P, C.c_int32, C.POINTER(nb_diagnostics)]),
@@ -221,6 +222,12 @@ def fp32_peak_tflops() -> float:
     v = C.c_double()
     _check(lib.nb_device_fp32_peak_tflops(C.byref(v)))
     return v.value
+
+
+def inject_alloc_failure(nth: int) -> None:
+    """Test hook: the nth device allocation of the library from now on fails with
+    NB_ERR_OUT_OF_MEMORY (0 disarms)."""
+    _check(lib.nb_inject_alloc_failure(nth))
 
 
 def num_kernel_configs() -> int:

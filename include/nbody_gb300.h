@@ -170,6 +170,12 @@ int nb_sim_advance_per_system(nb_sim* s, int32_t iterations);
  * nb_sim_synchronize / nb_sim_get_state returns NB_ERR_DEVICE_TIMEOUT.  No
  * memory is faulted and nothing hangs; the simulation stays usable. */
 int nb_sim_inject_wait_timeout(nb_sim* s);
+/* Failure-detection test hook, host side only: the `nth` device allocation the
+ * library makes from now on (1 = the next one, in any thread) fails with
+ * NB_ERR_OUT_OF_MEMORY without calling cudaMalloc; 0 disarms it.  Lets tests
+ * drive every clean-up path.  No reference counterpart (the reference exits on
+ * any CUDA error, simulator.cuh:22-31). */
+int nb_inject_alloc_failure(int32_t nth);
 /* Wait for the stream and report any device-side error (e.g. a wait that timed out). */
 int nb_sim_synchronize(nb_sim* s);
 /* Run `iterations` iterations bracketed by CUDA events on the simulation's stream

@@ -105,6 +105,17 @@ def test_invalid_arguments_rejected_before_device():
     with pytest.raises(nb.NbError) as e:
         nb.Simulation(nb.SimParam(), (x, y, z), (vx, vy, vz), m, sizes=[16, 0, 16])
     assert e.value.status == nb.NB_ERR_INVALID_ARGUMENT
+    with pytest.raises(nb.NbError) as e:
+        nb.Simulation(nb.SimParam(numParticles=32, accumulator=3), (x, y, z), (vx, vy, vz), m)
+    assert e.value.status == nb.NB_ERR_INVALID_ARGUMENT
+    assert "NB_ACC_REFERENCE_ORDER" in nb.lib.nb_last_error().decode()
+
+
+def test_alloc_failure_hook_arguments():
+    with pytest.raises(nb.NbError) as e:
+        nb.inject_alloc_failure(-1)
+    assert e.value.status == nb.NB_ERR_INVALID_ARGUMENT
+    nb.inject_alloc_failure(0)                          # disarmed: a no-op
 
 
 # ----------------------------------------------------------------- initial conditions

@@ -47,3 +47,44 @@ def test_errors_do_not_cross_the_abi_as_exceptions():
         assert e.value.status == nb.NB_ERR_STATE
         sim.advance(1)
         sim.synchronize()
+
+
+def test_every_allocation_failure_is_reported_and_cleaned_up():
+    """Fail the k-th device allocation of a simulation's creation and first use
+    (state, work list, reference-order tiles, accelerations, diagnostics, render
+    buffers) for every k: each failure surfaces as NB_ERR_OUT_OF_MEMORY, nothing
+    leaks into the next attempt, and once k passes the last allocation everything
+    works and matches the oracle."""
+    n = 3000
+    pos, vel, m = disk_case(n, seed=79)
+
+    import torch
+
+    img = torch.empty((64, 64, 4), dtype=torch.float32, device="cuda")
+    view, proj = nb.camera_matrices(0.0, 0.5, 8.0, 64, 64)
+
+    def use(acc):
+        with nb.Simulation(params(n, acc=acc), pos, vel, m) as sim:
+            sim.advance(1)
+            sim.accelerations()
+            sim.diagnostics()
+            sim.render(view, proj, 64, 64, img.data_ptr())
+            return sim.get_state()
+
+    for acc in (nb.ACC_PLAIN, nb.ACC_REFERENCE_ORDER):
+        failures = 0
+        for k in range(1, 200):
+            nb.inject_alloc_failure(k)
+            try:
+                got = use(acc)
+            except nb.NbError as e:
+                assert e.status == nb.NB_ERR_OUT_OF_MEMORY, (k, e)
+                failures += 1
+                continue
+            finally:
+                nb.inject_alloc_failure(0)
+            break
+        assert failures >= 5, failures           # creation alone makes several allocations
+        ref = orc.run_fp32(pos, vel, None, g_eff(1.0, m[0]), 1e-3, 0.999, 1e-3, iters=1)
+        scale = max(float(np.max(np.abs(r))) for r in ref[:3])
+        assert max(float(np.max(np.abs(g - r))) for g, r in zip(got[:3], ref[:3])) <= 1e-4 * scale
