@@ -291,3 +291,26 @@ def test_library_matches_golden_fixtures(name):
     else:
         scale = max(float(np.max(np.abs(r))) for r in out[:3])
         assert max(float(np.max(np.abs(g - r))) for g, r in zip(got[:3], out[:3])) <= POS_REL * scale
+
+
+@pytest.mark.parametrize("acc", [nb.ACC_PLAIN, nb.ACC_COMPENSATED])
+def test_coincident_particles_like_reference(acc):
+    """Tuned kernel on particles at identical positions: finite and within tolerance
+    of the oracle for eps > 0; NaN exactly for the coincident particles for eps = 0,
+    as the reference's 0 * rsqrt(0) gives."""
+    n = 600
+    pos, vel, m = disk_case(n, seed=21)
+    for a in pos:
+        a[300:310] = a[0]
+        a[500] = a[499]
+    with nb.Simulation(params(n, acc=acc), pos, vel, None) as sim:
+        got = sim.accelerations()
+    assert all(np.all(np.isfinite(g)) for g in got)
+    rms, mx = vec_errors(got, orc.accel_fp64(pos, None, 1.0, EPS32))
+    assert rms <= ACC_RMS and mx <= ACC_MAX
+    with nb.Simulation(params(n, eps=0.0, acc=acc), pos, vel, None) as sim:
+        got = sim.accelerations()
+    bad = np.isnan(got[0])
+    expect = np.zeros(n, bool)
+    expect[[0, *range(300, 310), 499, 500]] = True
+    assert np.array_equal(bad, expect)

@@ -125,3 +125,30 @@ def test_unequal_masses_are_rejected():
         with pytest.raises(nb.NbError) as e:
             sim.advance(1)
     assert e.value.status == nb.NB_ERR_INVALID_ARGUMENT
+
+
+@needs_reference
+@pytest.mark.parametrize("eps", [1e-3, 0.0])
+def test_coincident_particles_match_reference_kernel(eps):
+    """Particles at identical positions: with eps > 0 their mutual term is exactly
+    zero; with eps = 0 it is 0 * rsqrt(0) = NaN in the reference, and NaN must appear
+    in the same words here (NaN payloads aside)."""
+    n = 600
+    pos, vel, _ = disk_case(n, seed=21)
+    for a in pos:
+        a[300:310] = a[0]           # ten copies of particle 0's position
+        a[500] = a[499]
+    iters = 1 if eps == 0.0 else 2   # NaN positions would reach every particle in step 2
+    ref, _ = orc.reference_run(pos, vel, 1.0, 1e-3, 0.999, eps, iters=iters, method=orc.BRANCH)
+    with nb.Simulation(ro_params(n, eps=eps), pos, vel, None) as sim:
+        sim.advance(iters)
+        got = sim.get_state()
+    for g, r in zip(got, ref):
+        assert np.array_equal(np.isnan(g), np.isnan(r))
+        fin = ~np.isnan(r)
+        assert np.array_equal(g[fin].view(np.uint32), r[fin].view(np.uint32))
+    if eps == 0.0:
+        assert np.isnan(ref[3][0]) and np.isnan(ref[3][300]) and np.isnan(ref[3][500])
+        assert not np.isnan(ref[3][1])
+    else:
+        assert all(np.all(np.isfinite(r)) for r in ref)
