@@ -438,7 +438,8 @@ def bench_adjoint(args) -> dict:
 
 # --------------------------------------------------------------------------- precision study
 def run_precision_study(args) -> dict:
-    """Config 2: N = 262,144 two-disk collision, plain vs compensated FP32 accumulation.
+    """Config 2: N = 262,144 two-disk collision, plain vs compensated vs reference-order
+    (the reference kernel's own summation, bit for bit) FP32 accumulation.
     FP64 energy and momenta (GPU) and the force error against FP64 accelerations on
     sampled rows every `every` steps.  Damping is 1 so that energy is conserved by the
     dynamics and its drift measures the arithmetic."""
@@ -451,7 +452,8 @@ def run_precision_study(args) -> dict:
     out = {"study": "precision", "N": n, "steps": steps, "every": every, "eps2": eps, "dt": dt,
            "damping": 1.0, "G": 1.0, "seed": SEED, "rows_sampled": int(rows.size),
            "modes": {}}
-    for name, acc in (("plain", nb.ACC_PLAIN), ("compensated", nb.ACC_COMPENSATED)):
+    for name, acc in (("plain", nb.ACC_PLAIN), ("compensated", nb.ACC_COMPENSATED),
+                      ("reference_order", nb.ACC_REFERENCE_ORDER)):
         p = nb.SimParam(numParticles=n, G=1.0, dt=dt, damping=1.0, distEps=eps, accumulator=acc)
         sim = nb.Simulation(p, (x, y, z), (vx, vy, vz), m)
         series = []
@@ -493,7 +495,7 @@ def run_precision_study(args) -> dict:
 
 # --------------------------------------------------------------------------- accuracy study
 def run_accuracy_study(args) -> dict:
-    """Force error of both accumulators against FP64 for the initial state of each
+    """Force error of every accumulator against FP64 for the initial state of each
     configuration: FP32 accelerations of the library vs GPU FP64 accelerations on
     strided rows (for the ensemble: rows spread over all systems)."""
     import nbody_gb300 as nb
@@ -519,7 +521,8 @@ def run_accuracy_study(args) -> dict:
     for name, pos, vel, m, sizes_, eps in cases:
         n = pos[0].size
         res = {"N": int(n), "eps2": eps}
-        for acc_name, acc in (("plain", nb.ACC_PLAIN), ("compensated", nb.ACC_COMPENSATED)):
+        for acc_name, acc in (("plain", nb.ACC_PLAIN), ("compensated", nb.ACC_COMPENSATED),
+                              ("reference_order", nb.ACC_REFERENCE_ORDER)):
             p = nb.SimParam(G=1.0, dt=1e-3, damping=1.0, distEps=eps, accumulator=acc,
                             numParticles=n)
             sim = nb.Simulation(p, pos, vel, m, sizes=sizes_)
@@ -593,7 +596,7 @@ def main() -> int:
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--study", choices=["precision", "accuracy"], default=None,
                     help="run a study instead of the benchmark (precision: config 2 over time; "
-                         "accuracy: force error vs FP64 of every config, both accumulators)")
+                         "accuracy: force error vs FP64 of every config, every accumulator)")
     ap.add_argument("--study-steps", type=int, default=1000)
     ap.add_argument("--flush-mib", type=int, default=512,
                     help="L2 flush buffer written between timed steps (0: no flush; profiling)")
