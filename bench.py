@@ -215,6 +215,7 @@ def run_ours(args, rank, world) -> dict:
     stream = torch.cuda.current_stream()
     flush = torch.empty(max(1, args.flush_mib) << 20, dtype=torch.uint8, device="cuda")
     peak_tf = nb.fp32_peak_tflops()
+    peak_meas_tf = nb.measured_fp32_peak_tflops()
 
     # Every accumulator: force error against FP64 at the initial state, then the rate.
     modes = {}
@@ -273,6 +274,10 @@ def run_ours(args, rank, world) -> dict:
                     "traffic": traffic_from_profile(),
                     "peak_source": "nominal: SMs x 128 FP32 lanes x 2 flop x max SM clock "
                                    "(no FP32 peak in MEASURED_PEAKS.json)",
+                    "peak_measured": peak_meas_tf,
+                    "frac_of_measured": achieved_tf / peak_meas_tf,
+                    "peak_measured_source": "FFMA2 loop kernel over every SM, best of 10 "
+                                            "(nb_measure_fp32_peak_tflops), this run",
                     "flop_per_pair": FLOP_PER_PAIR,
                     "kernel_ms": {"min": min(step_ms), "median": statistics.median(step_ms)}}
         # e2e through the C ABI with pinned host buffers

@@ -35,7 +35,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-ftz=true", "-Xcompiler"
                      "-Xcompiler", "-ffp-contract=off"]
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall"]
 
-LIB_CU = ["force_shapes_a.cu", "force_shapes_b.cu", "force_shapes_c.cu", "force_kernel.cu", "reference_order_kernel.cu",
+LIB_CU = ["force_shapes_a.cu", "force_shapes_b.cu", "force_shapes_c.cu", "force_kernel.cu", "reference_order_kernel.cu", "peak_probe.cu",
           "aux_kernels.cu", "diag_kernels.cu", "adjoint_kernel.cu", "initgen.cu", "noalloc.cu",
           "render_kernels.cu"]
 LIB_CPP = ["nbody_capi.cpp", "nbody_aux.cpp", "nbody_render.cpp", "worklist.cpp",

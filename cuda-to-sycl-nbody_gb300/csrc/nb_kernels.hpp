@@ -32,6 +32,13 @@ cudaError_t reference_order_blocks_per_sm(int* blocks);
 cudaError_t launch_reference_order(const ForceArgs& a, const int32_t* tiles, int32_t num_tiles,
                                    int grid, cudaStream_t stream);
 
+// ---- measured FP32 throughput (peak_probe.cu) ----------------------------------------
+// Time `repeats` launches (after one warm-up) of an FFMA2 loop over sms x blocks_per_sm
+// CTAs; `scratch` holds sms * blocks_per_sm * fp32_peak_threads() float2.
+cudaError_t measure_fp32_peak(int sms, float2* scratch, int blocks_per_sm, int iters,
+                              int repeats, cudaStream_t stream, double* tflops, float* best_ms);
+int fp32_peak_threads();
+
 // ---- state movement (aux_kernels.cu) ------------------------------------------------
 // Device SoA staging <-> simulation layout.  `map` holds, for each of the n real
 // particles in user order, its padded device index.

@@ -554,6 +554,22 @@ int nb_device_fp32_peak_tflops(double* tflops) {
   return NB_OK;
 }
 
+int nb_measure_fp32_peak_tflops(double* tflops) {
+  if (!tflops) return set_error(NB_ERR_INVALID_ARGUMENT, "out is NULL");
+  int sms = 0;
+  cudaDeviceProp prop;
+  NB_TRY(check_device(&sms, &prop));
+  constexpr int kBlocksPerSm = 4, kIters = 4096, kRepeats = 10;
+  float2* scratch = nullptr;
+  NB_TRY(dev_alloc(&scratch, static_cast<size_t>(sms) * kBlocksPerSm * fp32_peak_threads()));
+  float ms = 0.f;
+  const cudaError_t e =
+      measure_fp32_peak(sms, scratch, kBlocksPerSm, kIters, kRepeats, nullptr, tflops, &ms);
+  dev_free(scratch);
+  if (e != cudaSuccess) return cuda_error(e, "measure_fp32_peak");
+  return NB_OK;
+}
+
 int nb_sim_create(const nb_params* p, const float* x, const float* y, const float* z,
                   const float* vx, const float* vy, const float* vz, const float* mass,
                   nb_sim** out) {

@@ -95,6 +95,7 @@ SIGNATURES = {
     "nb_params_parse_args": (C.c_int, [C.POINTER(nb_params), C.c_int, C.POINTER(C.c_char_p)]),
     "nb_device_name": (C.c_int, [C.c_char_p, C.c_size_t]),
     "nb_device_fp32_peak_tflops": (C.c_int, [_D]),
+    "nb_measure_fp32_peak_tflops": (C.c_int, [C.POINTER(C.c_double)]),
     "nb_sim_create": (C.c_int, [C.POINTER(nb_params)] + [_F] * 7 + [C.POINTER(_P)]),
     "nb_sim_create_disk_galaxy": (C.c_int, [C.POINTER(nb_params), C.POINTER(_P)]),
     "nb_ensemble_create": (C.c_int, [C.POINTER(nb_params), C.c_uint32, _U32] + [_F] * 7
@@ -228,6 +229,13 @@ def inject_alloc_failure(nth: int) -> None:
     """Test hook: the nth device allocation of the library from now on fails with
     NB_ERR_OUT_OF_MEMORY (0 disarms)."""
     _check(lib.nb_inject_alloc_failure(nth))
+
+
+def measured_fp32_peak_tflops() -> float:
+    """FP32 TFLOP/s of an FFMA2 loop kernel on the current device (measured)."""
+    v = C.c_double()
+    _check(lib.nb_measure_fp32_peak_tflops(C.byref(v)))
+    return v.value
 
 
 def num_kernel_configs() -> int:

@@ -74,3 +74,11 @@ def test_fp64_rows_match_oracle_rows():
     ref = orc.accel_fp64(pos, m, 1.0, EPS32, rows=rows.astype(np.int64))
     for a, b in zip(got, ref):
         assert np.allclose(a, b, rtol=1e-12, atol=1e-14)
+
+
+def test_measured_fp32_peak_is_close_to_nominal():
+    """The FFMA2 loop reaches most of the nominal FP32 rate and cannot exceed it by
+    more than clock-rounding slack."""
+    nominal = nb.fp32_peak_tflops()
+    measured = nb.measured_fp32_peak_tflops()
+    assert 0.5 * nominal < measured < 1.05 * nominal, (measured, nominal)
