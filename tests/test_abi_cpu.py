@@ -88,6 +88,11 @@ def test_no_device_is_reported_not_fatal():
     with pytest.raises(nb.NbError) as e:
         nb.device_name()
     assert e.value.status == nb.NB_ERR_NO_DEVICE
+    for fn in (nb.fp32_peak_tflops, nb.measured_fp32_peak_tflops):
+        with pytest.raises(nb.NbError) as e:
+            fn()
+        assert e.value.status == nb.NB_ERR_NO_DEVICE
+    assert nb.lib.nb_measure_fp32_peak_tflops(None) == nb.NB_ERR_INVALID_ARGUMENT
     (x, y, z), (vx, vy, vz), m = nb.thin_disk(1, 32, 1e-3)
     with pytest.raises(nb.NbError) as e:
         nb.Simulation(nb.SimParam(numParticles=32), (x, y, z), (vx, vy, vz), m)
