@@ -152,3 +152,28 @@ def test_coincident_particles_match_reference_kernel(eps):
         assert not np.isnan(ref[3][1])
     else:
         assert all(np.all(np.isfinite(r)) for r in ref)
+
+
+@needs_reference
+@pytest.mark.parametrize("seed", range(24))
+def test_random_cases_bitwise_equal_to_reference_kernel(seed):
+    """Seeded random sizes, softenings (zero included), G, dt, damping, iteration
+    counts and position scales: every output word equals the reference kernel's."""
+    rng = np.random.default_rng(1000 + seed)
+    n = int(rng.choice([1, 2, 3, 31, 32, 33, 255, 256, 257, 511, 1023, 1025]) if seed < 8
+            else rng.integers(1, 6000))
+    eps = float(np.float32([0.0, 1e-6, 1e-4, 1e-3, 1e-2, 0.1][seed % 6]))
+    G = float(np.float32(10 ** rng.uniform(-3, 1)))
+    dt = float(np.float32(10 ** rng.uniform(-4, -2)))
+    damping = float(np.float32(rng.choice([1.0, 0.999, 0.9])))
+    iters = int(rng.integers(1, 5))
+    scale = 10 ** rng.uniform(-1, 2)
+    pos = [(rng.standard_normal(n) * scale).astype(np.float32) for _ in range(3)]
+    vel = [(rng.standard_normal(n) * 0.1).astype(np.float32) for _ in range(3)]
+    ref, _ = orc.reference_run(pos, vel, G, dt, damping, eps, iters=iters, method=orc.BRANCH)
+    p = nb.SimParam(numParticles=n, G=G, dt=dt, damping=damping, distEps=eps,
+                    calcMethod=nb.BRANCH, accumulator=nb.ACC_REFERENCE_ORDER)
+    with nb.Simulation(p, pos, vel, None) as sim:
+        sim.advance(iters)
+        got = sim.get_state()
+    assert same_bits(got, ref), (n, eps, G, dt, damping, iters)
