@@ -276,7 +276,7 @@ def run_ours(args, rank, world) -> dict:
                                    "(no FP32 peak in MEASURED_PEAKS.json)",
                     "peak_measured": peak_meas_tf,
                     "frac_of_measured": achieved_tf / peak_meas_tf,
-                    "peak_measured_source": "FFMA2 loop kernel over every SM, best of 10 "
+                    "peak_measured_source": "FFMA2 loop kernel over every SM, best of 20 "
                                             "(nb_measure_fp32_peak_tflops), this run",
                     "flop_per_pair": FLOP_PER_PAIR,
                     "kernel_ms": {"min": min(step_ms), "median": statistics.median(step_ms)}}

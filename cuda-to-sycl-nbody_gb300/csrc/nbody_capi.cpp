@@ -559,7 +559,7 @@ int nb_measure_fp32_peak_tflops(double* tflops) {
   int sms = 0;
   cudaDeviceProp prop;
   NB_TRY(check_device(&sms, &prop));
-  constexpr int kBlocksPerSm = 4, kIters = 4096, kRepeats = 10;
+  constexpr int kBlocksPerSm = 4, kIters = 4096, kRepeats = 20;
   float2* scratch = nullptr;
   NB_TRY(dev_alloc(&scratch, static_cast<size_t>(sms) * kBlocksPerSm * fp32_peak_threads()));
   float ms = 0.f;

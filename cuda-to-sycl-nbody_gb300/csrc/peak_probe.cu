@@ -46,8 +46,14 @@ cudaError_t measure_fp32_peak(int sms, float2* scratch, int blocks_per_sm, int i
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaError_t e = cudaEventCreate(&e0);
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  // Warm-up: about 50 ms of the same work, so that the SM clock has settled before
+  // the timed launches (a first call from an idle GPU read 4 % low after 10 ms).
+  for (int r = 0; r < 100 && e == cudaSuccess; ++r) {
+    ffma2_peak_kernel<<<grid, kPeakThreads, 0, stream>>>(scratch, iters, a, b);
+    e = cudaGetLastError();
+  }
   float best = 1e30f;
-  for (int r = 0; r <= repeats && e == cudaSuccess; ++r) {  // r = 0 warms up
+  for (int r = 0; r <= repeats && e == cudaSuccess; ++r) {  // r = 0 is not counted
     e = cudaEventRecord(e0, stream);
     if (e == cudaSuccess) {
       ffma2_peak_kernel<<<grid, kPeakThreads, 0, stream>>>(scratch, iters, a, b);

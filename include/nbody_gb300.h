@@ -136,9 +136,9 @@ int nb_params_parse_args(nb_params* p, int argc, const char* const* argv);
 int nb_device_name(char* buf, size_t len);
 /* Nominal FP32 peak of device 0 in TFLOP/s: SMs x 128 lanes x 2 x max SM clock. */
 int nb_device_fp32_peak_tflops(double* tflops);
-/* Measured FP32 throughput of the current device in TFLOP/s: the best of 10
- * timed launches of a loop of independent packed FP32x2 fused multiply-adds
- * (FFMA2) over every SM, about 10 ms in all.  A measured denominator for the
+/* Measured FP32 throughput of the current device in TFLOP/s: the best of 20
+ * timed launches, after about 50 ms of warm-up, of a loop of independent packed
+ * FP32x2 fused multiply-adds (FFMA2) over every SM, about 65 ms in all.  A measured denominator for the
  * force kernel's efficiency, beside the nominal figure above.  No reference
  * counterpart. */
 int nb_measure_fp32_peak_tflops(double* tflops);
