@@ -10,10 +10,13 @@ host by the library's seeded generator (no dataset).
 Prints one JSON line.  `value` is device time with the state resident in HBM
 (CUDA events on the simulation's stream, L2 flushed between timed steps);
 `e2e` is the same metric through the C ABI with host buffers: every step copies
-the state in from pinned host memory, advances, and copies it back.  The CPU
-baseline times the oracle (the reference kernel body restated in C, OpenMP) on
-a bounded sample of i-rows against all N j-particles.  Extra keys report the
-ensemble and adjoint speed-ups of the metric's other two parts.
+the state in from pinned host memory, advances, and copies it back.  Every
+accumulator is measured (plain, compensated, and reference order -- the
+reference kernel's own summation, bit for bit); the headline is the fastest one
+whose force error against FP64 is within 1e-5 relative RMS.  The CPU baseline
+times the oracle (the reference kernel body restated in C, OpenMP) on a bounded
+sample of i-rows against all N j-particles.  Extra keys report the ensemble and
+adjoint speed-ups of the metric's other two parts, and the headless render.
 
 With --impl reference the line reports the reference's CPU path (the oracle
 port on all host threads) on the same workload, and -- as an extra key -- the

@@ -1,7 +1,8 @@
 // Host runtime behind the C ABI (include/nbody_gb300.h).
 //
 // One nb_sim owns the device state of one or more independent systems, a CUDA
-// stream, and the work lists of the persistent force kernel.  All calls are
+// stream, the work lists of the persistent force kernel and the tile table of
+// the reference-order kernel (NB_ACC_REFERENCE_ORDER).  All calls are
 // stream-ordered on that stream; the calls that return data to the host
 // synchronize it.  Errors are returned as nb_status codes with a thread-local
 // message; nothing here exits or throws across the ABI (the reference aborts on
