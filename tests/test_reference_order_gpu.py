@@ -177,3 +177,26 @@ def test_random_cases_bitwise_equal_to_reference_kernel(seed):
         sim.advance(iters)
         got = sim.get_state()
     assert same_bits(got, ref), (n, eps, G, dt, damping, iters)
+
+
+@needs_reference
+def test_thousand_steps_bitwise_equal_to_reference_kernel():
+    """1000 iterations of the config-0 disk (N = 25,600, unit masses with G = 1/N):
+    the trajectories are chaotic, so any single rounding difference would have
+    grown into visible divergence; every word still matches."""
+    n, iters = 25600, 1000
+    pos, vel, _ = disk_case(n, seed=2024)
+    G = float(np.float32(1.0 / n))
+    ref, _ = orc.reference_run(pos, vel, G, 1e-3, 0.999, 1e-3, iters=iters, method=orc.BRANCH)
+    p = nb.SimParam(numParticles=n, G=G, dt=1e-3, damping=0.999, distEps=1e-3,
+                    calcMethod=nb.BRANCH, accumulator=nb.ACC_REFERENCE_ORDER)
+    with nb.Simulation(p, pos, vel, None) as sim:
+        sim.advance(iters)
+        got = sim.get_state()
+    assert same_bits(got, ref)
+    # the tuned kernel follows a different rounding path and ends elsewhere
+    p.accumulator = nb.ACC_PLAIN
+    with nb.Simulation(p, pos, vel, None) as sim:
+        sim.advance(iters)
+        fast = sim.get_state()
+    assert not same_bits(fast, ref)
