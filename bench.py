@@ -154,6 +154,9 @@ def cpu_sample_rate(pos, mass_G, target_s: float, max_rows: int | None = None):
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_binding as orc
 
+    # Every core this process may run on (a launcher may have set OMP_NUM_THREADS=1).
+    orc.set_num_threads(len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity")
+                        else (os.cpu_count() or 1))
     n = pos[0].size
     rows = 64
     while True:

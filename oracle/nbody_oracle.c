@@ -182,3 +182,15 @@ int oracle_num_threads(void) {
   return 1;
 #endif
 }
+
+/* Threads for the parallel loops from now on (OpenMP's omp_set_num_threads); a
+ * launcher such as torchrun sets OMP_NUM_THREADS=1, and the CPU baseline wants
+ * every core it may use. */
+void oracle_set_num_threads(int n) {
+#ifdef _OPENMP
+  extern void omp_set_num_threads(int);
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}

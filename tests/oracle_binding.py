@@ -42,6 +42,8 @@ def lib() -> C.CDLL:
                                                                   C.c_int64] + [_D] * 3
         L.oracle_energy_fp64.argtypes = [C.c_int64] + [_F] * 7 + [C.c_double, C.c_double, _D]
         L.oracle_num_threads.restype = C.c_int
+        L.oracle_set_num_threads.argtypes = [C.c_int]
+        L.oracle_set_num_threads.restype = None
         L.oracle_render.argtypes = [C.c_int64] + [_F] * 7 + [C.c_int, C.c_int, _F, _F, C.c_int,
                                                               _F, C.c_int, _F]
         L.oracle_render.restype = C.c_int
@@ -59,6 +61,10 @@ def _p(a):
 
 def num_threads() -> int:
     return lib().oracle_num_threads()
+
+
+def set_num_threads(n: int) -> None:
+    lib().oracle_set_num_threads(int(n))
 
 
 def run_fp32(pos, vel, mass, G, dt, damping, eps, iters, method=BRANCH):
