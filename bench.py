@@ -321,7 +321,10 @@ def run_ours(args, rank, world) -> dict:
             "roofline": roofline, "e2e": e2e, "gpu_launches": args.steps,
             "clocks": clk.summary(), "wall_s_timed_region": wall,
         }
-    if rank == 0 and not args.no_extras:
+    # The extras and the CPU baseline run at N = 1 only: under torchrun they would hold
+    # every GPU of the job while rank 0 alone works.
+    solo = rank == 0 and world == 1
+    if solo and not args.no_extras:
         result["render"] = bench_render(modes[head]["sim"], n)
     result["accumulators"] = {k: {a: b for a, b in v.items() if a not in ("sim", "probe_ms")}
                               for k, v in modes.items()}
@@ -330,10 +333,10 @@ def run_ours(args, rank, world) -> dict:
     for v in modes.values():
         v["sim"].close()
     del flush
-    if rank == 0 and not args.no_extras:
+    if solo and not args.no_extras:
         result["ensemble"] = bench_ensemble(args)
         result["adjoint"] = bench_adjoint(args)
-    if rank == 0 and not args.no_cpu:
+    if solo and not args.no_cpu:
         rate, rows, secs, thr = cpu_sample_rate(pos, float(np.float32(m[0])), args.cpu_seconds)
         result["cpu_baseline"] = {
             "value": rate, "unit": UNIT, "cores": thr, "kind": "port",
