@@ -97,6 +97,21 @@ static int validate_params(const nb_params* p) {
 }
 
 // Recompute per-system mass mode and G scale from host masses (user order).
+constexpr const char* kReferenceOrderMassError =
+    "NB_ACC_REFERENCE_ORDER needs equal masses within each system (the reference has unit "
+    "masses)";
+
+// True when the masses (user order) are equal within every system, as the
+// reference-order kernel needs.
+static bool equal_masses_per_system(const nb_sim* s, const float* mass) {
+  for (size_t k = 0; k < s->sys_h.size(); ++k) {
+    const int64_t u0 = s->user_offset[k];
+    for (int32_t i = 1; i < s->sys_h[k].n; ++i)
+      if (mass[u0 + i] != mass[u0]) return false;
+  }
+  return true;
+}
+
 static void assign_mass_mode(nb_sim* s, const std::vector<float>& mass) {
   bool all_equal = true;
   for (size_t k = 0; k < s->sys_h.size(); ++k) {
@@ -312,10 +327,7 @@ int force_pass(nb_sim* s, float4* accel_out, bool per_system) {
     for (int32_t k = 0; k < static_cast<int32_t>(s->sys_h.size()); ++k)
       NB_CUDA(launch_predicated(a, s->sys_h[k], k, s->stream));
   } else if (s->params.accumulator == NB_ACC_REFERENCE_ORDER) {
-    if (s->per_pair_mass)
-      return set_error(NB_ERR_INVALID_ARGUMENT,
-                       "NB_ACC_REFERENCE_ORDER needs equal masses within each system (the "
-                       "reference has unit masses)");
+    if (s->per_pair_mass) return set_error(NB_ERR_INVALID_ARGUMENT, kReferenceOrderMassError);
     const int32_t nsys = static_cast<int32_t>(s->sys_h.size());
     if (per_system) {
       for (int32_t k = 0; k < nsys; ++k) NB_TRY(launch_reference_order_range(s, a, k, k + 1));
@@ -412,6 +424,10 @@ static int create_impl(const nb_params* p, uint32_t num_systems, const uint32_t*
   std::vector<float> m(total, 1.0f);
   if (mass) std::copy(mass, mass + total, m.begin());
   assign_mass_mode(s, m);
+  if (p->accumulator == NB_ACC_REFERENCE_ORDER && s->per_pair_mass) {
+    delete s;  // nothing on the device yet
+    return set_error(NB_ERR_INVALID_ARGUMENT, kReferenceOrderMassError);
+  }
 
   int st = NB_OK;
   auto fail = [&](int code) {
@@ -700,6 +716,9 @@ int nb_sim_set_state(nb_sim* s, const float* x, const float* y, const float* z, 
                      const float* vy, const float* vz, const float* mass) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
   DeviceGuard dg_(s->device);
+  if (mass && s->params.accumulator == NB_ACC_REFERENCE_ORDER &&
+      !equal_masses_per_system(s, mass))
+    return set_error(NB_ERR_INVALID_ARGUMENT, kReferenceOrderMassError);  // state unchanged
   if (mass) {
     std::vector<float> m(mass, mass + s->n_real);
     assign_mass_mode(s, m);

@@ -118,13 +118,21 @@ def test_accelerations_agree_with_oracle():
 
 
 def test_unequal_masses_are_rejected():
+    """At creation, and by set_state (which then leaves the state untouched)."""
     n = 64
     pos, vel, _ = disk_case(n, seed=4)
     m = np.linspace(1.0, 2.0, n).astype(np.float32)
-    with nb.Simulation(ro_params(n), pos, vel, m) as sim:
-        with pytest.raises(nb.NbError) as e:
-            sim.advance(1)
+    with pytest.raises(nb.NbError) as e:
+        nb.Simulation(ro_params(n), pos, vel, m)
     assert e.value.status == nb.NB_ERR_INVALID_ARGUMENT
+    with nb.Simulation(ro_params(n), pos, vel, None) as sim:
+        before = sim.get_state()
+        with pytest.raises(nb.NbError) as e:
+            sim.set_state(pos, vel, m)
+        assert e.value.status == nb.NB_ERR_INVALID_ARGUMENT
+        assert same_bits(sim.get_state(), before)
+        sim.set_state(pos, vel, np.full(n, 0.5, np.float32))   # equal masses: accepted
+        sim.advance(1)
 
 
 @needs_reference
