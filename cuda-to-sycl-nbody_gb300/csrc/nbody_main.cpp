@@ -4,7 +4,8 @@
 // per-step line on stdout.
 //
 // Two environment variables that the reference does not have:
-//   NBODY_GB300_ACCUMULATOR   plain | compensated | reference_order (default plain);
+//   NBODY_GB300_ACCUMULATOR   plain | compensated | reference_order (default
+//                             compensated);
 //                             reference_order gives the reference kernel's results bit
 //                             for bit
 //   NBODY_GB300_STATE_OUT     file that receives the final state as raw float32

@@ -181,7 +181,7 @@ class SimParam:
         p = nb_params()
         lib.nb_params_default(C.byref(p))
         self._from_c(p)
-        self.accumulator = ACC_PLAIN
+        self.accumulator = ACC_COMPENSATED  # the library default (nb_params_default)
         for k, v in kw.items():
             if k not in self.FIELDS and k != "accumulator":
                 raise TypeError(f"unknown SimParam field {k}")
