@@ -25,12 +25,13 @@ cudaError_t launch_predicated(const ForceArgs& a, const SystemDesc& sd, int32_t 
 // ---- reference-order force + integrate (reference_order_kernel.cu) -------------------
 // particle_interaction<BRANCH> with the reference's per-particle summation order
 // and arithmetic (bit-identical results on the same GPU), equal masses per system.
-// `tiles` holds (system, i-tile) pairs of reference_order_tile() i-particles.
-int reference_order_tile();
-KernelShape reference_order_shape();  // threads, i-particles per thread, j-tile, 2 buffers
-cudaError_t reference_order_blocks_per_sm(int* blocks);
-cudaError_t launch_reference_order(const ForceArgs& a, const int32_t* tiles, int32_t num_tiles,
-                                   int grid, cudaStream_t stream);
+// Shapes are indexed largest i-tile first; `tiles` holds (system, i-tile) pairs of
+// reference_order_shape(index).bi() i-particles.
+int reference_order_num_shapes();
+KernelShape reference_order_shape(int index);  // threads, i-particles per thread, j-tile, 2
+cudaError_t reference_order_blocks_per_sm(int index, int* blocks);
+cudaError_t launch_reference_order(int index, const ForceArgs& a, const int32_t* tiles,
+                                   int32_t num_tiles, int grid, cudaStream_t stream);
 
 // ---- measured FP32 throughput (peak_probe.cu) ----------------------------------------
 // Time `repeats` launches (after one warm-up) of an FFMA2 loop over sms x blocks_per_sm

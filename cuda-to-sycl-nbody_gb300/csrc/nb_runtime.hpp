@@ -87,8 +87,9 @@ struct nb_sim {
   int32_t* counters_d = nullptr;
   size_t counters_cap = 0;
 
-  // NB_ACC_REFERENCE_ORDER: (system, i-tile) pairs of the reference-order kernel,
-  // the first tile of each system (systems + 1 entries) and its grid.
+  // NB_ACC_REFERENCE_ORDER: the reference-order kernel's shape, its (system, i-tile)
+  // pairs, the first tile of each system (systems + 1 entries) and its grid.
+  int ro_shape = 0;
   int32_t* ro_tiles_d = nullptr;
   std::vector<int32_t> ro_first;
   int ro_grid = 0;

@@ -256,10 +256,30 @@ static int build_per_system_worklists(nb_sim* s) {
   return NB_OK;
 }
 
-// Tile table of the reference-order kernel (built once, at creation: the
-// systems never change afterwards).
+// i-tiles of all systems for reference-order shape `shape`.
+static int32_t reference_order_tile_count(const nb_sim* s, int shape) {
+  const int bi = reference_order_shape(shape).bi();
+  int64_t tiles = 0;
+  for (const SystemDesc& d : s->sys_h) tiles += (d.n + bi - 1) / bi;
+  return static_cast<int32_t>(std::min<int64_t>(tiles, INT32_MAX));
+}
+
+// Default reference-order shape: the largest i-tiles that still give every SM at
+// least one tile (a particle's sum is never split, so a small system needs small
+// tiles to occupy the GPU); the smallest shape when none does.  Measured against the
+// fastest shape: N = 2,048 .. 65,536 take 64 x 1, N = 262,144 and 1M take 128 x 4.
+static int default_reference_order_shape(const nb_sim* s) {
+  const int last = reference_order_num_shapes() - 1;
+  for (int k = 0; k < last; ++k)
+    if (reference_order_tile_count(s, k) >= s->sms) return k;
+  return last;
+}
+
+// Tile table of the reference-order kernel for shape s->ro_shape (rebuilt when the
+// shape changes; the systems never change after creation).
 static int build_reference_order_tiles(nb_sim* s) {
-  const int bi = reference_order_tile();
+  const int bi = reference_order_shape(s->ro_shape).bi();
+  dev_free(s->ro_tiles_d);
   std::vector<int32_t> t;
   s->ro_first.assign(1, 0);
   for (int32_t k = 0; k < static_cast<int32_t>(s->sys_h.size()); ++k) {
@@ -275,7 +295,8 @@ static int build_reference_order_tiles(nb_sim* s) {
                           cudaMemcpyHostToDevice, s->stream));
   NB_CUDA(cudaStreamSynchronize(s->stream));  // the host vector dies on return
   int blocks = 0;
-  if (reference_order_blocks_per_sm(&blocks) != cudaSuccess || blocks < 1) blocks = 1;
+  if (reference_order_blocks_per_sm(s->ro_shape, &blocks) != cudaSuccess || blocks < 1)
+    blocks = 1;
   s->ro_grid = blocks * s->sms;
   return NB_OK;
 }
@@ -284,7 +305,8 @@ static int build_reference_order_tiles(nb_sim* s) {
 static int launch_reference_order_range(nb_sim* s, const ForceArgs& a, int32_t k0, int32_t k1) {
   const int32_t first = s->ro_first[k0];
   const int32_t count = s->ro_first[k1] - first;
-  NB_CUDA(launch_reference_order(a, s->ro_tiles_d + 2 * static_cast<int64_t>(first), count,
+  NB_CUDA(launch_reference_order(s->ro_shape, a,
+                                 s->ro_tiles_d + 2 * static_cast<int64_t>(first), count,
                                  std::min(s->ro_grid, count), s->stream));
   return NB_OK;
 }
@@ -469,6 +491,7 @@ static int create_impl(const nb_params* p, uint32_t num_systems, const uint32_t*
     return fail(cuda_error(e, "copy state"));
   s->cfg = default_config(s);
   if ((st = build_main_worklist(s, s->cfg)) != NB_OK) return fail(st);
+  s->ro_shape = default_reference_order_shape(s);
   if ((st = build_reference_order_tiles(s)) != NB_OK) return fail(st);
   if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return fail(cuda_error(e, "create"));
   *out = s;
@@ -829,10 +852,10 @@ int nb_sim_set_kernel_config(nb_sim* s, int32_t index) {
 int nb_sim_kernel_info(const nb_sim* s, nb_kernel_info* info) {
   if (!s || !info) return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
   if (s->params.accumulator == NB_ACC_REFERENCE_ORDER) {
-    const KernelShape sh = reference_order_shape();
+    const KernelShape sh = reference_order_shape(s->ro_shape);
     const int32_t tiles = s->ro_first.empty() ? 0 : s->ro_first.back();
-    *info = nb_kernel_info{-1, sh.threads, sh.r, sh.bj, sh.stages, std::min(s->ro_grid, tiles),
-                           tiles, 0};
+    *info = nb_kernel_info{-1 - s->ro_shape, sh.threads, sh.r, sh.bj, sh.stages,
+                           std::min(s->ro_grid, tiles), tiles, 0};
     return NB_OK;
   }
   const KernelShape sh = force_config_shape(s->cfg);
@@ -844,12 +867,37 @@ int nb_sim_kernel_info(const nb_sim* s, nb_kernel_info* info) {
 int nb_sim_autotune(nb_sim* s, int32_t* chosen) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
   DeviceGuard dg_(s->device);
-  if (s->params.calc_method == NB_PREDICATED || s->params.accumulator == NB_ACC_REFERENCE_ORDER) {
-    // These modes run kernels of one fixed shape: nothing to choose.
+  if (s->params.calc_method == NB_PREDICATED) {
+    // The compatibility kernel has one fixed shape: nothing to choose.
     if (chosen) *chosen = s->cfg;
     return NB_OK;
   }
   NB_TRY(ensure_accel(s));
+  if (s->params.accumulator == NB_ACC_REFERENCE_ORDER) {
+    // Time the reference-order shapes (accelerations only; every shape gives the
+    // same bits) and keep the fastest.
+    int best = s->ro_shape;
+    float best_ms = 1e30f;
+    for (int k = 0; k < reference_order_num_shapes(); ++k) {
+      s->ro_shape = k;
+      NB_TRY(build_reference_order_tiles(s));
+      NB_TRY(force_pass(s, s->acc_d, false));  // warm-up
+      NB_CUDA(cudaEventRecord(s->ev0, s->stream));
+      NB_TRY(force_pass(s, s->acc_d, false));
+      NB_CUDA(cudaEventRecord(s->ev1, s->stream));
+      NB_CUDA(cudaEventSynchronize(s->ev1));
+      float ms = 0.f;
+      NB_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = k;
+      }
+    }
+    s->ro_shape = best;
+    NB_TRY(build_reference_order_tiles(s));
+    if (chosen) *chosen = -1 - best;
+    return NB_OK;
+  }
   int best = s->cfg;
   float best_ms = 1e30f;
   for (int c = 0; c < num_force_configs(); ++c) {

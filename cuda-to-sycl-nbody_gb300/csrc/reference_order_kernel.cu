@@ -28,19 +28,17 @@
 namespace nbg {
 namespace {
 
-constexpr int kRoThreads = 128;  // threads per CTA
-constexpr int kRoPairs = 4;      // i-pairs per thread (8 i-particles)
-constexpr int kRoBI = kRoThreads * 2 * kRoPairs;  // i-particles per tile
+// Shapes: kRoThreads threads per CTA, kRoPairs i-pairs per thread, so i-tiles of
+// kRoThreads * 2 * kRoPairs particles.  A particle's sum cannot be split, so small
+// systems need small i-tiles to give every SM work (see the shape table below).
 constexpr int kRoBJ = 256;       // j-particles per shared-memory tile
 constexpr int kRoRecs = kRoBJ / 2;                // 32-byte pair records per j-tile
-constexpr int kRoRecsPerThread = (kRoRecs + kRoThreads - 1) / kRoThreads;
 constexpr int kRoUnroll = 4;     // j steps per unrolled block
-static_assert(kRoBI % kPadQuantum == 0, "i-tiles must hold whole padding quanta");
 
 // One j step against all of the thread's i-pairs.  kDiag: the tile overlaps the
 // i-tile, so the term of j == i is left out of that lane's sum (the reference's
 // `if (i == id) continue;`), by keeping the old value rather than adding zero.
-template <bool kDiag>
+template <int kRoPairs, bool kDiag>
 __device__ __forceinline__ void ro_step(const float4 xy, const float4 zm, float2 e2,
                                         const float2 (&nx)[kRoPairs],
                                         const float2 (&ny)[kRoPairs],
@@ -91,7 +89,7 @@ __device__ __forceinline__ void ro_step(const float4 xy, const float4 zm, float2
 }
 
 // Steps over j = j0 .. j0 + count - 1 of the staged tile, in order.
-template <bool kDiag>
+template <int kRoPairs, bool kDiag>
 __device__ __forceinline__ void ro_tile(const float4* __restrict__ tile, int count, int j0,
                                         float2 e2, const float2 (&nx)[kRoPairs],
                                         const float2 (&ny)[kRoPairs],
@@ -103,12 +101,12 @@ __device__ __forceinline__ void ro_tile(const float4* __restrict__ tile, int cou
   for (; jj + kRoUnroll <= count; jj += kRoUnroll) {
 #pragma unroll
     for (int u = 0; u < kRoUnroll; ++u)
-      ro_step<kDiag>(tile[2 * (jj + u)], tile[2 * (jj + u) + 1], e2, nx, ny, nz, ax, ay, az,
+      ro_step<kRoPairs, kDiag>(tile[2 * (jj + u)], tile[2 * (jj + u) + 1], e2, nx, ny, nz, ax, ay, az,
                      j0 + jj + u, li);
   }
 #pragma unroll 1
   for (; jj < count; ++jj)
-    ro_step<kDiag>(tile[2 * jj], tile[2 * jj + 1], e2, nx, ny, nz, ax, ay, az, j0 + jj, li);
+    ro_step<kRoPairs, kDiag>(tile[2 * jj], tile[2 * jj + 1], e2, nx, ny, nz, ax, ay, az, j0 + jj, li);
 }
 
 struct RoTile {
@@ -116,9 +114,13 @@ struct RoTile {
   int32_t itile;
 };
 
+template <int kRoThreads, int kRoPairs>
 __global__ void __launch_bounds__(kRoThreads) reference_order_kernel(const ForceArgs a,
                                                                       const RoTile* tiles,
                                                                       int32_t num_tiles) {
+  constexpr int kRoBI = kRoThreads * 2 * kRoPairs;  // i-particles per tile
+  constexpr int kRoRecsPerThread = (kRoRecs + kRoThreads - 1) / kRoThreads;
+  static_assert(kRoBI % kPadQuantum == 0, "i-tiles must hold whole padding quanta");
   // [buffer][j][2]: (x, x, y, y), (z, z, m, m)
   __shared__ __align__(16) float4 sm[2][kRoBJ * 2];
   const int tid = threadIdx.x;
@@ -187,9 +189,9 @@ __global__ void __launch_bounds__(kRoThreads) reference_order_kernel(const Force
       const int count = min(kRoBJ, sd.n - j0);
       const bool diag = (j0 < ibase + kRoBI) && (ibase < j0 + count);
       if (diag)
-        ro_tile<true>(sm[buf], count, j0, e2, nx, ny, nz, ax, ay, az, li);
+        ro_tile<kRoPairs, true>(sm[buf], count, j0, e2, nx, ny, nz, ax, ay, az, li);
       else
-        ro_tile<false>(sm[buf], count, j0, e2, nx, ny, nz, ax, ay, az, li);
+        ro_tile<kRoPairs, false>(sm[buf], count, j0, e2, nx, ny, nz, ax, ay, az, li);
       if (jt + 1 < ntiles_j) stage(jt + 1, buf ^ 1);
       __syncthreads();
     }
@@ -206,22 +208,40 @@ __global__ void __launch_bounds__(kRoThreads) reference_order_kernel(const Force
   }
 }
 
+struct RoShapeEntry {
+  int threads;
+  int pairs;
+  void (*kernel)(const ForceArgs, const RoTile*, int32_t);
+};
+
+// Largest i-tiles first.  Measured at N = 1M: 128 x 4 64.4 %, 128 x 2 62.8 % of FP32
+// peak; the 64 x 1 shape gives a 25,600-particle system 200 CTAs instead of 25.
+const RoShapeEntry kRoShapes[] = {
+    {128, 4, reference_order_kernel<128, 4>},
+    {128, 2, reference_order_kernel<128, 2>},
+    {64, 1, reference_order_kernel<64, 1>},
+};
+constexpr int kNumRoShapes = sizeof(kRoShapes) / sizeof(kRoShapes[0]);
+
 }  // namespace
 
-int reference_order_tile() { return kRoBI; }
+int reference_order_num_shapes() { return kNumRoShapes; }
 
-KernelShape reference_order_shape() { return KernelShape{kRoThreads, 2 * kRoPairs, kRoBJ, 2}; }
-
-cudaError_t reference_order_blocks_per_sm(int* blocks) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, reference_order_kernel, kRoThreads,
-                                                       0);
+KernelShape reference_order_shape(int index) {
+  const RoShapeEntry& e = kRoShapes[index];
+  return KernelShape{e.threads, 2 * e.pairs, kRoBJ, 2};
 }
 
-cudaError_t launch_reference_order(const ForceArgs& a, const int32_t* tiles, int32_t num_tiles,
-                                   int grid, cudaStream_t stream) {
+cudaError_t reference_order_blocks_per_sm(int index, int* blocks) {
+  const RoShapeEntry& e = kRoShapes[index];
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, e.kernel, e.threads, 0);
+}
+
+cudaError_t launch_reference_order(int index, const ForceArgs& a, const int32_t* tiles,
+                                   int32_t num_tiles, int grid, cudaStream_t stream) {
   if (num_tiles <= 0) return cudaSuccess;
-  reference_order_kernel<<<grid, kRoThreads, 0, stream>>>(
-      a, reinterpret_cast<const RoTile*>(tiles), num_tiles);
+  const RoShapeEntry& e = kRoShapes[index];
+  e.kernel<<<grid, e.threads, 0, stream>>>(a, reinterpret_cast<const RoTile*>(tiles), num_tiles);
   return cudaGetLastError();
 }
 

@@ -92,8 +92,9 @@ typedef struct nb_diagnostics {
 } nb_diagnostics;
 
 /* Kernel shape selected for a simulation (see nb_sim_autotune). */
-/* For NB_ACC_REFERENCE_ORDER, config_index is -1 and the fields describe the
- * reference-order kernel (segments = its i-tiles, no split tiles). */
+/* For NB_ACC_REFERENCE_ORDER, config_index is -1 - (reference-order shape) and the
+ * fields describe the reference-order kernel (segments = its i-tiles, no split
+ * tiles). */
 typedef struct nb_kernel_info {
   int32_t config_index;
   int32_t threads_per_block;
@@ -223,8 +224,9 @@ int nb_kernel_config_info(int32_t index, nb_kernel_info* info);
 int nb_sim_set_kernel_config(nb_sim* s, int32_t index);
 int nb_sim_kernel_info(const nb_sim* s, nb_kernel_info* info);
 /* Time every kernel shape on this simulation's data (accelerations only, the
- * state is not advanced) and keep the fastest; `chosen` may be NULL.  A no-op
- * for NB_PREDICATED and NB_ACC_REFERENCE_ORDER, whose kernels have one shape. */
+ * state is not advanced) and keep the fastest; `chosen` may be NULL.  With
+ * NB_ACC_REFERENCE_ORDER it times that kernel's shapes (all give the same bits)
+ * and reports -1 - shape; a no-op for NB_PREDICATED, whose kernel has one shape. */
 int nb_sim_autotune(nb_sim* s, int32_t* chosen);
 
 /* Plan the work list of kernel shape `config_index` for systems of the given

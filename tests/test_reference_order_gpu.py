@@ -208,3 +208,27 @@ def test_thousand_steps_bitwise_equal_to_reference_kernel():
         sim.advance(iters)
         fast = sim.get_state()
     assert not same_bits(fast, ref)
+
+
+@needs_reference
+@pytest.mark.parametrize("n", [25600, 300000])
+def test_every_shape_and_autotune_stay_bitwise(n):
+    """The default shape depends on the size (small systems get small i-tiles);
+    the autotuner picks among all shapes; every choice gives the reference's bits."""
+    pos, vel, _ = disk_case(n, seed=31)
+    G = float(np.float32(1.0 / n))
+    ref, _ = orc.reference_run(pos, vel, G, 1e-3, 0.999, 1e-3, iters=2, method=orc.BRANCH)
+    p = nb.SimParam(numParticles=n, G=G, dt=1e-3, damping=0.999, distEps=1e-3,
+                    calcMethod=nb.BRANCH, accumulator=nb.ACC_REFERENCE_ORDER)
+    with nb.Simulation(p, pos, vel, None) as sim:
+        default = sim.kernel_info()["config_index"]
+        chosen = sim.autotune()
+        assert chosen <= -1 and sim.kernel_info()["config_index"] == chosen
+        sim.advance(2)
+        got = sim.get_state()
+    assert default <= -1
+    if n == 25600:
+        assert default == -3          # 64 x 1: 200 tiles instead of 25
+    else:
+        assert default == -1          # 128 x 4: 293 tiles, more than one per SM
+    assert same_bits(got, ref)
