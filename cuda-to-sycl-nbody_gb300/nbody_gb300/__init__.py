@@ -483,6 +483,9 @@ class Simulation:
         return {f: getattr(k, f) for f, _ in nb_kernel_info._fields_}
 
     def autotune(self) -> int:
+        """Time the kernel shapes on this simulation's data and keep the fastest.
+        Returns the tuned kernel's config index, or -1 - shape for the
+        reference-order kernel (NB_ACC_REFERENCE_ORDER)."""
         v = C.c_int32()
         _check(lib.nb_sim_autotune(self._h, C.byref(v)))
         return v.value
