@@ -54,3 +54,30 @@ def test_two_gloo_ranks_aggregate_like_the_benchmark():
     for _, _, slowest, rate in out:
         assert slowest == 2.0                     # max over ranks
         assert rate == pytest.approx(2 * 1000.0 / 4.0)
+
+
+def test_reference_arm_json_contract():
+    """`bench.py --impl reference` runs on host cores only, so its whole JSON line can
+    be checked here: the keys and meanings the benchmark contract asks for."""
+    import json
+    import subprocess
+
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "3", "--cpu-seconds", "0.5"],
+                       capture_output=True, text=True, timeout=600, cwd=str(ROOT))
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
+                "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["value"] > 0 and line["unit"] == "pair-interactions/s"
+    assert line["steps"] == 1 and line["warmup"] >= 3 and line["higher_is_better"] is True
+    assert line["config"]["workload"].startswith("Plummer sphere N=1048576")
+    cb = line["cpu_baseline"]
+    assert cb["value"] == line["value"] and cb["kind"] == "port" and cb["cores"] >= 1
+    assert cb["sample"]
+    e2e = line["e2e"]
+    assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
+    assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
