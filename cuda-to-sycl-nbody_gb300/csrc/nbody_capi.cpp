@@ -383,21 +383,29 @@ int check_error_word(nb_sim* s) {
   return NB_OK;
 }
 
-static int default_config(const nb_sim* s) {
-  // Large systems: 256 x 4 with 2048-particle j-tiles (one CTA per SM); ensembles of
-  // small systems: 256 x 2 with 256-particle j-tiles.
-  int64_t sum_n2 = 0, sum_n3 = 0;
-  for (const auto& d : s->sys_h) {
-    sum_n2 += static_cast<int64_t>(d.n) * d.n;
-    sum_n3 += static_cast<int64_t>(d.n) * d.n / 64 * d.n / 64;
+// Default kernel shape: the one with the largest tiles whose work list still gives
+// every CTA at least 16 (i-tile, j-tile) blocks, so that the stream-K split balances
+// to within a few percent; the smallest shape otherwise.  Deterministic (the
+// autotuner may pick otherwise, and shapes round differently).  Measured against
+// the autotuner's pick: N = 25,600 -> 256 x 2 x 256 (0.24 ms, the 1M shape takes
+// 0.32), 65,536 -> 256 x 4 x 1024, 262,144 and 1M -> 256 x 4 x 2048.
+static int default_config(nb_sim* s) {
+  static const int kCandidates[] = {9, 8, 10, 3, 4};  // largest tiles first
+  for (const int cfg : kCandidates) {
+    const KernelShape sh = force_config_shape(cfg);
+    int64_t blocks = 0;
+    for (const auto& d : s->sys_h) {
+      const int64_t i_tiles = (d.n + sh.bi() - 1) / sh.bi();
+      blocks += i_tiles * ((d.npad + sh.bj - 1) / sh.bj);
+    }
+    if (blocks >= 16 * static_cast<int64_t>(max_grid_for(s, cfg))) return cfg;
   }
-  const double weighted_n = sum_n2 ? static_cast<double>(sum_n3) * 4096.0 / sum_n2 : 0.0;
-  return weighted_n >= 16384.0 ? 9 : 3;
+  return 4;
 }
 
-static int create_impl(const nb_params* p, uint32_t num_systems, const uint32_t* sizes, const float* x,
-                const float* y, const float* z, const float* vx, const float* vy, const float* vz,
-                const float* mass, nb_sim** out) {
+static int create_impl(const nb_params* p, uint32_t num_systems, const uint32_t* sizes,
+                       const float* x, const float* y, const float* z, const float* vx,
+                       const float* vy, const float* vz, const float* mass, nb_sim** out) {
   if (!out) return set_error(NB_ERR_INVALID_ARGUMENT, "out is NULL");
   *out = nullptr;
   NB_TRY(validate_params(p));
@@ -459,7 +467,8 @@ static int create_impl(const nb_params* p, uint32_t num_systems, const uint32_t*
   cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) return fail(cuda_error(e, "cudaStreamCreate"));
   s->own_stream = true;
-  if ((e = cudaEventCreate(&s->ev0)) != cudaSuccess || (e = cudaEventCreate(&s->ev1)) != cudaSuccess)
+  if ((e = cudaEventCreate(&s->ev0)) != cudaSuccess ||
+      (e = cudaEventCreate(&s->ev1)) != cudaSuccess)
     return fail(cuda_error(e, "cudaEventCreate"));
   if ((st = dev_alloc(&s->sys_d, s->sys_h.size())) != NB_OK) return fail(st);
   if ((st = dev_alloc(&s->pos_d[0], 4 * static_cast<size_t>(s->n_pad))) != NB_OK) return fail(st);
