@@ -121,6 +121,9 @@ typedef struct nb_segment {
 typedef struct nb_sim nb_sim; /* opaque */
 
 /* ---- errors --------------------------------------------------------------- */
+/* Replace gpuErrchk's print-and-exit (simulator.cuh:22-31): the message of the
+ * calling thread's last failed call, the name of a status code, and the ABI
+ * version (no reference counterpart). */
 const char* nb_last_error(void);
 const char* nb_status_string(int status);
 int nb_abi_version(void);
@@ -208,7 +211,8 @@ int nb_sim_last_step_ms(const nb_sim* s, float* ms);
 int nb_sim_gw_size(const nb_sim* s, int32_t* gw);
 int nb_sim_calc_method(const nb_sim* s, int32_t* method);
 
-/* Use `stream` for all later work of this simulation (NULL = legacy default). */
+/* Use `stream` for all later work of this simulation (NULL = legacy default).  The
+ * reference always uses the default stream (simulator.cu:67, 80, 107). */
 int nb_sim_set_stream(nb_sim* s, void* stream);
 /* Device hand-off replacing the per-frame host copy to the renderer
  * (RendererGL::updateParticles, renderer_gl.cpp:111-114, 156-172): writes the
@@ -218,6 +222,9 @@ int nb_sim_set_stream(nb_sim* s, void* stream);
 int nb_sim_export_device(nb_sim* s, float* pos_xyzm_device, float* vel_xyzw_device);
 
 /* ---- kernel selection ---------------------------------------------------------- */
+/* The compiled shapes of the tuned kernel.  No reference counterpart: the
+ * reference launches ceil(N / gwSize) blocks of gwSize threads (simulator.cu:49-50),
+ * and gwSize is only reported here (nb_sim_gw_size). */
 int nb_num_kernel_configs(void);
 int nb_kernel_config_info(int32_t index, nb_kernel_info* info);
 /* Select a kernel shape by index (-1 = the built-in default for this size). */
@@ -242,12 +249,16 @@ int nb_plan_work(uint32_t num_systems, const uint32_t* sizes, int32_t config_ind
                  int32_t* num_partial_slots);
 
 /* ---- CUDA graphs ------------------------------------------------------------------ */
+/* No reference counterpart: stepSim launches every iteration itself
+ * (simulator.cu:57-66). */
 /* Capture `iterations` iterations into a CUDA graph (replacing any earlier one). */
 int nb_sim_graph_capture(nb_sim* s, int32_t iterations);
 /* Launch the captured graph once on the simulation's stream. */
 int nb_sim_graph_launch(nb_sim* s);
 
 /* ---- FP64 diagnostics ---------------------------------------------------------- */
+/* No reference counterpart: the reference reports only kernel times
+ * (nbody.cpp:108-123). */
 /* Energy and momenta of system `system` (-1 = all systems together, without the
  * cross-system potential).  FP64 pair arithmetic and reductions on the GPU. */
 int nb_sim_diagnostics(nb_sim* s, int32_t system, nb_diagnostics* out);
@@ -257,6 +268,8 @@ int nb_sim_fp64_accelerations(nb_sim* s, const uint64_t* rows, uint64_t count,
                               double* ax, double* ay, double* az);
 
 /* ---- adjoint ----------------------------------------------------------------------- */
+/* No reference counterpart: gradients of the reference's T-iteration map
+ * (simulator.cu:186-229 applied T times) with respect to the initial state. */
 /* Run T iterations forward from the current state, keeping a checkpoint of
  * (x, v) every `checkpoint_every` iterations for nb_sim_adjoint_backward. */
 int nb_sim_adjoint_forward(nb_sim* s, int32_t T, int32_t checkpoint_every);
@@ -316,6 +329,8 @@ typedef enum nb_ic_kind { NB_IC_THIN_DISK = 1, NB_IC_PLUMMER = 2, NB_IC_TWO_DISK
 int nb_sim_generate(nb_sim* s, int32_t kind, uint64_t seed);
 
 /* ---- initial conditions (host, seeded, deterministic) -------------------------------- */
+/* No reference counterpart: the workloads' generators.  The reference's own
+ * initial state is nb_ic_reference_disk / nb_sim_create_disk_galaxy. */
 /* Thin disk: r = sqrt(u), theta uniform, z ~ N(0, 0.01^2), tangential speed
  * r * sqrt(n m r^2 / (r^2 + eps)^1.5) + N(0, 0.01) per component, m = 1/n. */
 int nb_ic_thin_disk(uint64_t seed, uint64_t n, float eps, float* x, float* y, float* z,
