@@ -37,10 +37,14 @@ def test_energy_and_momentum_drift_no_worse_than_reference():
         ref, _ = orc.reference_run(pos, vel, g_eff(1.0, m[0]), 1e-3, 1.0, 1e-3, STEPS)
         de_ref, dp_ref = drifts(diag, ref, m, e0, p0, scale)
         results = {}
-        for name, acc in (("plain", nb.ACC_PLAIN), ("compensated", nb.ACC_COMPENSATED)):
+        for name, acc in (("plain", nb.ACC_PLAIN), ("compensated", nb.ACC_COMPENSATED),
+                          ("reference order", nb.ACC_REFERENCE_ORDER)):
             with nb.Simulation(params(N, damping=1.0, acc=acc), pos, vel, m) as sim:
                 sim.advance(STEPS)
                 st = sim.get_state()
+            if acc == nb.ACC_REFERENCE_ORDER:   # the reference's own trajectory, bit for bit
+                assert all(np.array_equal(a.view(np.uint32), b.view(np.uint32))
+                           for a, b in zip(st, ref))
             results[name] = drifts(diag, st, m, e0, p0, scale)
     print(f"reference kernel: energy drift {de_ref:.3e}, momentum drift {dp_ref:.3e}")
     for name, (de, dp) in results.items():
