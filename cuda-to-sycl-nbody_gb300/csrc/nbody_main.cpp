@@ -1,5 +1,5 @@
-// Headless driver: the reference's no_render main loop (src/nbody.cpp:138-248 with
-// DISABLE_GL) on the GB300 simulator.  Same positional arguments
+// Headless driver: the reference's no_render main (src/nbody.cpp:31-36 construction,
+// :83-123 the DISABLE_GL frame loop) on the GB300 simulator.  Same positional arguments
 // (nBatches iters damping dt distEps G numFrames gwSize calcMethod) and the same
 // per-step line on stdout.
 //
@@ -63,11 +63,14 @@ int main(int argc, char** argv) {
       const size_t warmSteps = 2;
       if (step > warmSteps) {
         stepTimes.push_back(nbodySim.getLastStepTime());
-        const float cum = std::accumulate(stepTimes.begin(), stepTimes.end(), 0.0f);
+        // The same arithmetic as src/nbody.cpp:110-118: the sum is taken in double
+        // (initial value 0.0) and stored as float; each squared deviation comes
+        // from std::pow in double and is added into a float.
+        const float cum = std::accumulate(stepTimes.begin(), stepTimes.end(), 0.0);
         const float mean = cum / stepTimes.size();
         float acc = 0.0f;
-        for (float t : stepTimes) acc += (t - mean) * (t - mean);
-        const float sd = std::sqrt(acc / stepTimes.size());
+        for (const float t : stepTimes) acc += std::pow(t - mean, 2);
+        const float sd = std::pow(acc / stepTimes.size(), 0.5);
         std::cout << "At step " << step << " kernel time is " << stepTimes.back()
                   << " and mean is " << mean << " and stddev is: " << sd << "\n";
       }

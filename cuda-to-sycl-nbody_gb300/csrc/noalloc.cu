@@ -14,8 +14,10 @@
 // word -- lives in one file-scope device array, kScratchBytes (13 MiB) long.
 // Every GPU that loads this module keeps that array until the process exits.
 // All calls share it and it keeps the last call's contents: each call clears
-// what must start at zero (the counters and the error word), and calls whose
-// kernels overlap on the GPU (e.g. on two streams) race on it.
+// what must start at zero (the counters and the error word).  Two calls whose
+// work overlapped on the GPU would race on it, so each call holds a process-wide
+// lock from its first copy until its stream has drained: the calls of one
+// process run one after another, whatever streams and threads they come from.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -28,6 +30,7 @@
 #include "nb_kernels.hpp"
 #include "nb_runtime.hpp"
 #include "nbody_gb300.h"
+#include "worklist.hpp"
 
 namespace nbg {
 
@@ -37,18 +40,27 @@ constexpr int kNaConfig = 0;                  // kernel shape: 128 threads x 4 i
 constexpr int kNaBI = 512;                    // i-particles per CTA of that shape
 constexpr int kNaBJ = 256;                    // j-particles per tile of that shape
 constexpr int64_t kNaMaxParticles = 1 << 18;  // 262,144
-constexpr int kNaMaxGrid = 1024;
-constexpr int kNaMaxSegments = 2048;
-constexpr int kNaMaxSlots = 1024;
+constexpr int kNaMaxItiles = static_cast<int>(kNaMaxParticles / kNaBI);
+// Persistent CTAs: the occupancy limit of the shape (two per SM on GB300), capped
+// at four per SM of a 152-SM part; a smaller grid only balances less finely.
+constexpr int kNaMaxGrid = 608;
+// Bounds of a plan over at most kNaMaxItiles i-tiles on at most kNaMaxGrid CTAs
+// (worklist.hpp): every CTA boundary inside an i-tile adds one segment, each
+// segment of a split i-tile takes one partial-sum slot, and an i-tile is split
+// only by a CTA boundary.
+constexpr int kNaMaxSegments = kNaMaxItiles + kNaMaxGrid - 1;
+constexpr int kNaMaxSlots = kNaMaxSegments;
+constexpr int kNaMaxFixups = kNaMaxItiles < kNaMaxGrid - 1 ? kNaMaxItiles : kNaMaxGrid - 1;
 constexpr int kNaMaxDevices = 64;
+static_assert(kNaMaxParticles % kNaBI == 0, "whole i-tiles at the maximum size");
 
 constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
 constexpr size_t kOffSys = 0;
 constexpr size_t kOffErr = 256;
 constexpr size_t kOffCounters = 512;
-constexpr size_t kOffFix = align256(kOffCounters + sizeof(int32_t) * kNaMaxGrid);
-constexpr size_t kOffBegin = align256(kOffFix + sizeof(Fixup) * kNaMaxGrid);
+constexpr size_t kOffFix = align256(kOffCounters + sizeof(int32_t) * kNaMaxFixups);
+constexpr size_t kOffBegin = align256(kOffFix + sizeof(Fixup) * kNaMaxFixups);
 constexpr size_t kOffSegs = align256(kOffBegin + sizeof(int32_t) * (kNaMaxGrid + 1));
 constexpr size_t kOffPos = align256(kOffSegs + sizeof(Segment) * kNaMaxSegments);
 constexpr size_t kOffPartials = align256(kOffPos + 16 * kNaMaxParticles);
@@ -86,7 +98,32 @@ std::mutex g_na_mutex;                       // guards the host-side tables belo
 DeviceSetup g_na_setup[kNaMaxDevices];
 Segment g_na_segs[kNaMaxSegments];           // host plan, uploaded every call
 int32_t g_na_begin[kNaMaxGrid + 1];
-Fixup g_na_fix[kNaMaxGrid];
+Fixup g_na_fix[kNaMaxFixups];
+
+// The fixed host tables as the planner's output (worklist.hpp); refuses to grow.
+struct FixedTables {
+  int64_t grid = 0;
+  int64_t nseg = 0;
+  int64_t nfix = 0;
+  bool set_grid(int64_t g) {
+    grid = g;
+    return g >= 1 && g <= kNaMaxGrid;
+  }
+  bool add_segment(const Segment& sg) {
+    if (nseg >= kNaMaxSegments) return false;
+    g_na_segs[nseg++] = sg;
+    return true;
+  }
+  Segment& segment(int64_t i) { return g_na_segs[i]; }
+  int64_t num_segments() const { return nseg; }
+  void set_begin(int64_t cta, int64_t first) { g_na_begin[cta] = static_cast<int32_t>(first); }
+  bool add_fixup(const Fixup& f) {
+    if (nfix >= kNaMaxFixups) return false;
+    g_na_fix[nfix++] = f;
+    return true;
+  }
+  int64_t num_fixups() const { return nfix; }
+};
 
 // Once per device, with that device current: the scratch's device address and
 // the persistent grid size.
@@ -113,51 +150,21 @@ int na_setup(int dev, DeviceSetup* out) {
   return NB_OK;
 }
 
-// The stream-K plan of the force kernel (same rule as plan_worklist) for one
-// system, written into the fixed host tables.  Returns false if they are too small.
+// The force kernel's stream-K plan (plan_work_into, the rule of every other
+// launch) for one system, written into the fixed host tables.  The bounds above
+// make it fit for every n <= kNaMaxParticles and grid <= kNaMaxGrid; false if not.
 bool na_plan(int32_t n, int32_t npad, int32_t grid_max, int32_t* grid, int32_t* nseg,
              int32_t* nfix, int32_t* nslots) {
-  const int64_t nit = (n + kNaBI - 1) / kNaBI;
-  const int64_t njt = (npad + kNaBJ - 1) / kNaBJ;
-  const int64_t total = nit * npad;
-  const int64_t g = std::max<int64_t>(1, std::min<int64_t>(grid_max, nit * njt));
-  int32_t segs = 0, fix = 0, slots = 0;
-  int64_t next_cta = 0;
-  for (int64_t it = 0; it < nit; ++it) {
-    const int64_t c0 = it * npad;
-    const int32_t first = segs;
-    int64_t t = 0;
-    while (t < njt) {
-      const int64_t k = std::min<int64_t>(g - 1, ((c0 + t * kNaBJ) * g) / total);
-      int64_t t_end = njt;
-      if (k + 1 < g) {
-        const int64_t need = (k + 1) * total - c0 * g;
-        t_end = (need + static_cast<int64_t>(kNaBJ) * g - 1) / (static_cast<int64_t>(kNaBJ) * g);
-        t_end = std::min<int64_t>(std::max<int64_t>(t_end, t + 1), njt);
-      }
-      if (segs >= kNaMaxSegments) return false;
-      while (next_cta <= k) g_na_begin[next_cta++] = segs;
-      g_na_segs[segs++] = Segment{0, static_cast<int32_t>(it), static_cast<int32_t>(t),
-                                  static_cast<int32_t>(t_end), -1, 0};
-      t = t_end;
-    }
-    const int32_t parts = segs - first;
-    if (parts > 1) {
-      if (fix >= kNaMaxGrid || slots + parts > kNaMaxSlots) return false;
-      g_na_fix[fix] = Fixup{parts, slots};
-      for (int32_t p = 0; p < parts; ++p) {
-        g_na_segs[first + p].fix = fix;
-        g_na_segs[first + p].part = p;
-      }
-      ++fix;
-      slots += parts;
-    }
-  }
-  while (next_cta <= g) g_na_begin[next_cta++] = segs;
-  *grid = static_cast<int32_t>(g);
-  *nseg = segs;
-  *nfix = fix;
-  *nslots = slots;
+  SystemDesc sd{};
+  sd.n = n;
+  sd.npad = npad;
+  FixedTables out;
+  int32_t split = 0;
+  if (!plan_work_into(&sd, 0, 1, kNaBI, kNaBJ, grid_max, out, nslots, &split)) return false;
+  if (*nslots > kNaMaxSlots) return false;
+  *grid = static_cast<int32_t>(out.grid);
+  *nseg = static_cast<int32_t>(out.nseg);
+  *nfix = static_cast<int32_t>(out.nfix);
   return true;
 }
 
@@ -213,7 +220,7 @@ extern "C" int nb_accelerations_noalloc(const float* pos_xyzm_device, uint64_t n
     NB_CUDA(cudaMemcpyAsync(base + kOffFix, g_na_fix, sizeof(Fixup) * nfix,
                             cudaMemcpyHostToDevice, st));
   // What must start at zero: the arrival counters and the error word.
-  NB_CUDA(cudaMemsetAsync(base + kOffCounters, 0, sizeof(int32_t) * kNaMaxGrid, st));
+  NB_CUDA(cudaMemsetAsync(base + kOffCounters, 0, sizeof(int32_t) * kNaMaxFixups, st));
   NB_CUDA(cudaMemsetAsync(base + kOffErr, 0, sizeof(int32_t), st));
   float* pos = reinterpret_cast<float*>(base + kOffPos);
   na_to_pair_layout<<<(npad + 255) / 256, 256, 0, st>>>(

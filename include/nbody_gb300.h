@@ -291,9 +291,12 @@ int nb_sim_adjoint_backward(nb_sim* s, const float* gx_T, const float* gv_T,
  * fixed 13 MiB device array inside the library, which limits n to 262,144
  * (larger n: NB_ERR_INVALID_ARGUMENT) and which every GPU that loads the library
  * keeps until the process exits.  The first call on a device looks that array up
- * and should come before any stream capture.  All calls share the array:
- * calls whose work overlaps on the GPU (e.g. on two streams at once) race.  Runs
- * on `stream` and waits for it before returning. */
+ * and should come before any stream capture.  All calls share the array, which
+ * keeps the last call's contents (each call clears what must start at zero); calls
+ * whose work overlapped on the GPU would race on it, so each call holds a
+ * process-wide lock until its work has finished: calls from several threads or
+ * streams of one process run one after another.  Runs on `stream` and waits for
+ * it before returning. */
 int nb_accelerations_noalloc(const float* pos_xyzm_device, uint64_t n, float G, float dist_eps,
                              float* accel_xyzw_device, void* stream);
 

@@ -1,5 +1,5 @@
 /* A plain C99 caller of the C ABI, driving the library the way the reference's
- * main loop drives DiskGalaxySimulator (src/nbody.cpp:140-230): parse the same
+ * main loop drives DiskGalaxySimulator (src/nbody.cpp:31-36, 83-123): parse the same
  * positional arguments, build the reference's disk, step, read the state back.
  * Built and run by tests/test_c_abi_cpu.py and tests/test_c_abi_gpu.py. */
 #include <stdio.h>

@@ -238,6 +238,45 @@ def test_plan_work_covers_every_tile_once(sizes, cfg, grid):
         assert [p for _, p in sorted(v)] == list(range(len(v)))
 
 
+# The fixed tables of nb_accelerations_noalloc (csrc/noalloc.cu): kernel shape 0,
+# at most 262,144 particles (512 i-tiles of 512) on at most 608 persistent CTAs.
+NOALLOC_CFG, NOALLOC_MAX_N, NOALLOC_MAX_GRID = 0, 262144, 608
+NOALLOC_MAX_SEGMENTS = NOALLOC_MAX_SLOTS = 512 + NOALLOC_MAX_GRID - 1
+NOALLOC_MAX_FIXUPS = 512
+
+
+def _plan_counts(n, cfg, grid):
+    import ctypes as C
+
+    sz = np.array([n], dtype=np.uint32)
+    g, nseg, nfix, slots = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+    assert nb.lib.nb_plan_work(1, sz.ctypes.data_as(C.POINTER(C.c_uint32)), cfg, grid, None, 0,
+                               None, C.byref(g), C.byref(nseg), C.byref(nfix),
+                               C.byref(slots)) == nb.NB_OK
+    return g.value, nseg.value, nfix.value, slots.value
+
+
+def test_plan_size_bounds_hold_for_every_grid_of_the_noalloc_tables():
+    """Replays the planner of every launch (the one nb_accelerations_noalloc uses,
+    into its fixed tables) for each grid up to the entry point's cap, at the
+    maximum size and at sizes whose plans are the most fragmented, and checks the
+    bounds the fixed tables are sized by: segments <= i-tiles + grid - 1, slots <=
+    segments, fixups <= min(i-tiles, grid - 1)."""
+    info = nb.kernel_config_info(NOALLOC_CFG)
+    bi = info["threads_per_block"] * info["particles_per_thread"]
+    sizes = [NOALLOC_MAX_N, NOALLOC_MAX_N - 1, 214356, 131072 + 17, 65536, 12962, 5003, 513,
+             512, 17, 1]
+    for n in sizes:
+        nit = (n + bi - 1) // bi
+        for grid in range(1, NOALLOC_MAX_GRID + 1):
+            g, nseg, nfix, slots = _plan_counts(n, NOALLOC_CFG, grid)
+            assert g <= grid
+            assert nseg <= nit + g - 1, (n, grid, nseg)
+            assert slots <= nseg and nfix <= min(nit, g - 1), (n, grid, slots, nfix)
+            assert nseg <= NOALLOC_MAX_SEGMENTS and slots <= NOALLOC_MAX_SLOTS
+            assert nfix <= NOALLOC_MAX_FIXUPS
+
+
 def test_null_handles_are_rejected_without_touching_the_device():
     import ctypes as C
 

@@ -1,5 +1,5 @@
 """The headless no_render driver (csrc/nbody_main.cpp over csrc/simulator.cpp):
-the reference's argv and per-step stdout line (src/nbody.cpp:138-248)."""
+the reference's argv and per-step stdout line (src/nbody.cpp:31-36, 83-123)."""
 from __future__ import annotations
 
 import re
