@@ -14,13 +14,15 @@ the state in from pinned host memory, advances, and copies it back.  Every
 accumulator is measured (plain, compensated, and reference order -- the
 reference kernel's own summation, bit for bit); the headline is the fastest one
 whose force error against FP64 is within 1e-5 relative RMS.  The CPU baseline
-times the oracle (the reference kernel body restated in C, OpenMP) on a bounded
-sample of i-rows against all N j-particles.  Extra keys report the ensemble and
-adjoint speed-ups of the metric's other two parts, and the headless render.
+times the reference kernel body as an OpenMP loop built for speed
+(oracle/cpu_port.c, -O3 -ffast-math) on a bounded sample of i-rows against all N
+j-particles.  Extra keys report the ensemble and adjoint speed-ups of the metric's
+other two parts, and the headless render.
 
-With --impl reference the line reports the reference's CPU path (the oracle
-port on all host threads) on the same workload, and -- as an extra key -- the
-reference's own CUDA kernel built from its source for sm_103a.
+With --impl reference the line reports the reference's CPU path (that port, on
+all host threads) on the same workload -- made by the oracle's bit-identical
+restatement of the generator, so that arm never loads the library -- and, as an
+extra key, the reference's own CUDA kernel built from its source for sm_103a.
 """
 from __future__ import annotations
 
@@ -148,24 +150,29 @@ def whole_job_rate(units_per_rank: float, seconds_this_rank: float, world: int) 
     return units_per_rank * world / max_over_ranks(seconds_this_rank, world)
 
 
+CPU_PORT_DESC = ("oracle/cpu_port.c: the reference kernel body (src/simulator.cu:193-211) "
+                 "as an OpenMP loop over i-rows, built gcc -O3 -ffast-math -fopenmp (the j loop "
+                 "vectorised; no -march=native, one recipe for both hosts)")
+
+
 def cpu_sample_rate(pos, mass_G, target_s: float, max_rows: int | None = None):
-    """Oracle (FP32 restatement, OpenMP) on strided i-rows against all N j.
-    Returns (pairs/s, rows, seconds, threads)."""
+    """The timed CPU port on strided i-rows against all N j, on every core this
+    process may use.  Returns (pairs/s, rows, seconds, threads)."""
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_binding as orc
 
     # Every core this process may run on (a launcher may have set OMP_NUM_THREADS=1).
-    orc.set_num_threads(len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity")
-                        else (os.cpu_count() or 1))
+    orc.port_set_num_threads(len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity")
+                             else (os.cpu_count() or 1))
     n = pos[0].size
     rows = 64
     while True:
         idx = np.linspace(0, n - 1, rows).astype(np.int64)
         t0 = time.perf_counter()
-        orc.accel_fp32(pos, None, mass_G, EPS2, rows=idx)
+        orc.port_accel(pos, mass_G, EPS2, rows=idx)
         dt = time.perf_counter() - t0
         if dt >= target_s or (max_rows and rows >= max_rows):
-            return rows * n / dt, rows, dt, orc.num_threads()
+            return rows * n / dt, rows, dt, orc.port_num_threads()
         grow = max(2.0, min(8.0, target_s / max(dt, 1e-3)))
         rows = int(rows * grow)
         if max_rows:
@@ -173,9 +180,20 @@ def cpu_sample_rate(pos, mass_G, target_s: float, max_rows: int | None = None):
 
 
 def plummer_inputs(n=N_BENCH):
+    """The workload from the library's seeded generator (nb_ic_plummer)."""
     import nbody_gb300 as nb
 
     (x, y, z), (vx, vy, vz), m = nb.plummer(SEED, n)
+    return [x, y, z], [vx, vy, vz], m
+
+
+def plummer_inputs_without_library(n=N_BENCH):
+    """The same workload, bit for bit, from the oracle's restatement of the generator
+    (oracle/workload_ic.c): the reference arm never loads the library under test."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_binding as orc
+
+    (x, y, z), (vx, vy, vz), m = orc.plummer(SEED, n)
     return [x, y, z], [vx, vy, vz], m
 
 
@@ -341,8 +359,7 @@ def run_ours(args, rank, world) -> dict:
         result["cpu_baseline"] = {
             "value": rate, "unit": UNIT, "cores": thr, "kind": "port",
             "sample": f"{rows} strided i-rows x all {n} j-particles of the same workload "
-                      f"({secs:.1f} s), oracle/nbody_oracle.c (FP32 restatement of "
-                      "src/simulator.cu:186-229), OpenMP"}
+                      f"({secs:.1f} s) on {thr} threads; {CPU_PORT_DESC}"}
     return result
 
 
@@ -415,41 +432,72 @@ def bench_ensemble(args) -> dict:
     t1.record(stream)
     t1.synchronize()
     graph_ms = t0.elapsed_time(t1) / 100
+    # The baseline: one launch per system (the reference's stepSim launches one grid
+    # for its one system), each planned with the shape the system gets as a
+    # simulation of its own.  Also reported: every system with the ensemble's shape.
+    iters = 10
     sim.advance_per_system(1)
-    per_sys_ms = sim.time_iterations(3, per_system=True) / 3
+    per_sys_ms = sim.time_iterations(iters, per_system=1) / iters
+    sim.time_iterations(1, per_system=2)
+    per_sys_same_ms = sim.time_iterations(iters, per_system=2) / iters
     info = sim.kernel_info()
     sim.close()
     return {"systems": int(len(sizes)), "particles": int(sizes.sum()), "pairs_per_step": pairs,
             "persistent_ms_per_step": persistent_ms, "graph_ms_per_step": graph_ms,
+            "graph_steps_timed": 100,
             "per_system_launch_ms_per_step": per_sys_ms,
+            "per_system_policy": "one launch per system, each with the kernel shape it gets "
+                                 "as a simulation of its own (nb_sim_advance_per_system)",
+            "per_system_steps_timed": iters,
             "speedup_vs_per_system_launches": per_sys_ms / graph_ms,
+            "per_system_launch_ensemble_shape_ms_per_step": per_sys_same_ms,
+            "speedup_vs_per_system_launches_ensemble_shape": per_sys_same_ms / graph_ms,
             "pair_interactions_per_s": pairs / (graph_ms * 1e-3), "autotuned_config": chosen,
             "kernel": info}
 
 
 def bench_adjoint(args) -> dict:
-    """Config 4: N = 16,384 disk, T = 256 iterations, checkpoints every 16."""
+    """Config 4: N = 16,384 disk, T = 256 iterations, checkpoints every 16.  Forward
+    and backward are both timed with CUDA events on the simulation's stream; the
+    backward runs on device-resident gradients (nb_sim_adjoint_backward_device)."""
+    import torch
+
     import nbody_gb300 as nb
 
-    n, T, every = 16384, 256, 16
+    n, T, every, repeats = 16384, 256, 16, 3
     (x, y, z), (vx, vy, vz), m = nb.thin_disk(SEED, n, 1e-3)
     p = nb.SimParam(numParticles=n, G=1.0, dt=1e-3, damping=0.999, distEps=1e-3)
     sim = nb.Simulation(p, (x, y, z), (vx, vy, vz), m)
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
     sim.advance(2)
-    fwd_ms = sim.time_iterations(T) / T
+    fwd = [sim.time_iterations(T) / T for _ in range(repeats)]
     sim.set_state((x, y, z), (vx, vy, vz))
-    gx = np.ones(3 * n, dtype=np.float32) / n
+    gx = torch.full((3 * n,), 1.0 / n, dtype=torch.float32, device="cuda")
+    out = [torch.empty(3 * n, dtype=torch.float32, device="cuda") for _ in range(2)]
+    torch.cuda.synchronize()
     sim.adjoint_forward(T, every)
-    sim.adjoint_backward(gx)               # warm-up (allocations)
-    w = time.perf_counter()
-    sim.adjoint_backward(gx)
-    bwd_s = time.perf_counter() - w
+    sim.adjoint_backward_device(gx.data_ptr(), None, out[0].data_ptr(), out[1].data_ptr())
+    sim.synchronize()                      # warm-up
+    bwd = []
+    for _ in range(repeats):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.adjoint_backward_device(gx.data_ptr(), None, out[0].data_ptr(), out[1].data_ptr())
+        e1.record(stream)
+        e1.synchronize()
+        bwd.append(e0.elapsed_time(e1) / T)
+    sim.synchronize()
     sim.close()
-    per_step = bwd_s * 1e3 / T
-    return {"N": n, "T": T, "checkpoint_every": every, "forward_ms_per_step": fwd_ms,
-            "backward_ms_per_step": per_step,
-            "adjoint_step_cost_vs_forward": per_step / fwd_ms,
-            "note": "backward = recompute from checkpoints + VJP kernel, per step"}
+    fwd_ms, bwd_ms = statistics.median(fwd), statistics.median(bwd)
+    return {"N": n, "T": T, "checkpoint_every": every, "repeats": repeats,
+            "forward_ms_per_step": fwd_ms, "forward_ms_per_step_all": fwd,
+            "backward_ms_per_step": bwd_ms, "backward_ms_per_step_all": bwd,
+            "adjoint_step_cost_vs_forward": bwd_ms / fwd_ms,
+            "note": "medians of CUDA-event times on the simulation's stream; backward = "
+                    "recompute from checkpoints + VJP kernel per step, gradients resident "
+                    "on the device"}
 
 
 # --------------------------------------------------------------------------- precision study
@@ -557,29 +605,30 @@ def run_reference(args, rank, world) -> dict | None:
     import oracle_binding as orc
 
     n = args.n
-    pos, vel, m = plummer_inputs(n)
+    pos, vel, m = plummer_inputs_without_library(n)
     G = float(np.float32(m[0]))
     # size each step to ~ cpu_seconds / (steps + warmup) of work
     per_step_s = max(1.0, args.cpu_seconds * 2 / max(1, args.steps + args.warmup))
     rate0, rows, _, thr = cpu_sample_rate(pos, G, per_step_s)
     idx = np.linspace(0, n - 1, rows).astype(np.int64)
     for _ in range(args.warmup):
-        orc.accel_fp32(pos, None, G, EPS2, rows=idx)
+        orc.port_accel(pos, G, EPS2, rows=idx)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        orc.accel_fp32(pos, None, G, EPS2, rows=idx)
+        orc.port_accel(pos, G, EPS2, rows=idx)
         times.append(time.perf_counter() - t0)
     total = sum(times)
     value = rows * n * args.steps / total
-    sample = (f"{rows} strided i-rows x all {n} j-particles per step, oracle/nbody_oracle.c "
-              "(the reference kernel body src/simulator.cu:186-229 restated in C; the reference "
-              "ships no CPU path and its SYCL twin needs a DPC++ toolchain absent here), OpenMP")
+    sample = (f"{rows} strided i-rows x all {n} j-particles per step on {thr} threads; "
+              f"{CPU_PORT_DESC}.  The reference ships no CPU path, and its SYCL twin needs a "
+              "DPC++ toolchain that is absent here")
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": total * 1e3 / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-           "data": "synthetic (seeded Plummer sphere generated by the library)",
+           "data": "synthetic (seeded Plummer sphere; the oracle's bit-identical restatement of "
+                   "the library's generator)",
            "config": workload_desc(n),
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": thr, "kind": "port",
                             "sample": sample},
@@ -589,11 +638,16 @@ def run_reference(args, rank, world) -> dict | None:
         try:
             zeros = [np.zeros(n, np.float32)] * 3
             orc.reference_run(pos, zeros, G, DT, 1.0, EPS2, 1, gw_size=128)  # warm-up
-            _, ms = orc.reference_run(pos, zeros, G, DT, 1.0, EPS2, 1, gw_size=128)
+            launches = [orc.reference_run(pos, zeros, G, DT, 1.0, EPS2, 1, gw_size=128)[1]
+                        for _ in range(5)]
+            ms = statistics.median(launches)
             out["reference_cuda_kernel"] = {
                 "value": float(n) * n / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+                "ms_per_launch_all": launches, "ms_spread": max(launches) - min(launches),
+                "launches_timed": len(launches),
                 "source": "src/simulator.cu particle_interaction<BRANCH> compiled unmodified "
-                          "for sm_103a with -use_fast_math, gwSize 128, CUDA events"}
+                          "for sm_103a with -use_fast_math, gwSize 128; median of 5 single "
+                          "launches, CUDA events"}
         except Exception as e:  # reported, not fatal
             out["reference_cuda_kernel"] = {"unavailable": str(e).splitlines()[0]}
     return out

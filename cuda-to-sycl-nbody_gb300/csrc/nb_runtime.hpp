@@ -81,7 +81,7 @@ struct nb_sim {
   int cfg = 0;
   nbg::WorkListDev wl;
   std::vector<nbg::WorkListDev> wl_sys;
-  int wl_sys_cfg = -1;
+  int wl_sys_cfg = -1;  // shape of wl_sys (-2: each system's own default shape)
   float4* partials_d = nullptr;
   size_t partials_cap = 0;
   int32_t* counters_d = nullptr;
@@ -166,9 +166,15 @@ void dev_free(T*& p) {
 
 // Shared by the host translation units (nbody_capi.cpp).
 ForceArgs base_args(nb_sim* s);
+// How force_pass launches an ensemble: one persistent launch over every system,
+// or one launch per system, each planned with the shape the system would get as a
+// simulation of its own, or each with the simulation's current shape.
+constexpr int kPerSystemNone = 0;
+constexpr int kPerSystemOwnShape = 1;
+constexpr int kPerSystemSimShape = 2;
 // One force evaluation over all systems: integrate into the other position
 // buffer and swap (accel_out == nullptr), or write accelerations.
-int force_pass(nb_sim* s, float4* accel_out, bool per_system);
+int force_pass(nb_sim* s, float4* accel_out, int per_system);
 int check_error_word(nb_sim* s);
 int ensure_staging(nb_sim* s);
 int ensure_accel(nb_sim* s);

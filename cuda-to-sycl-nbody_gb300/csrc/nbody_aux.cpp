@@ -198,27 +198,20 @@ int nb_sim_adjoint_forward(nb_sim* s, int32_t T, int32_t checkpoint_every) {
   return NB_OK;
 }
 
-int nb_sim_adjoint_backward(nb_sim* s, const float* gx_T, const float* gv_T, float* gx_0,
-                            float* gv_0) {
-  if (!s || !gx_T || !gx_0 || !gv_0) return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
-  DeviceGuard dg_(s->device);
+// The backward sweep, stream-ordered on the simulation's stream, from device
+// gradients dL/dx_T, dL/dv_T (n x 3, xyz-interleaved; gv_T may be NULL) to device
+// dL/dx_0, dL/dv_0.  The outputs may alias the inputs: the inputs are read first.
+static int adjoint_backward_stream(nb_sim* s, const float* gx_T, const float* gv_T, float* gx_0,
+                                   float* gv_0) {
   AdjointState& a = s->adj;
-  if (!a.valid) return set_error(NB_ERR_STATE, "call nb_sim_adjoint_forward first");
-  NB_TRY(ensure_staging(s));
   const size_t n = s->n_real;
   const size_t np = static_cast<size_t>(s->n_pad);
-  float* stage = s->staging_d;  // 7n floats: room for one n x 3 array and more
   NB_CUDA(cudaMemsetAsync(a.lam_x, 0, np * sizeof(float4), s->stream));
   NB_CUDA(cudaMemsetAsync(a.lam_v, 0, np * sizeof(float4), s->stream));
   NB_CUDA(cudaMemsetAsync(a.tmp, 0, np * sizeof(float4), s->stream));
   NB_CUDA(cudaMemsetAsync(a.mu, 0, np * sizeof(float4), s->stream));
-  NB_CUDA(cudaMemcpyAsync(stage, gx_T, 3 * n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-  NB_CUDA(launch_unpack_vec3(stage, n, s->map_d, a.lam_x, s->stream));
-  if (gv_T) {
-    NB_CUDA(
-        cudaMemcpyAsync(stage, gv_T, 3 * n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    NB_CUDA(launch_unpack_vec3(stage, n, s->map_d, a.lam_v, s->stream));
-  }
+  NB_CUDA(launch_unpack_vec3(gx_T, n, s->map_d, a.lam_x, s->stream));
+  if (gv_T) NB_CUDA(launch_unpack_vec3(gv_T, n, s->map_d, a.lam_v, s->stream));
   const float dt = s->params.dt;
   for (int32_t k = a.count - 1; k >= 0; --k) {
     const int32_t t0 = k * a.every;
@@ -258,13 +251,39 @@ int nb_sim_adjoint_backward(nb_sim* s, const float* gx_T, const float* gv_T, flo
       std::swap(a.lam_v, a.mu);
     }
   }
-  NB_CUDA(launch_pack_vec3(a.lam_x, n, s->map_d, stage, s->stream));
+  NB_CUDA(launch_pack_vec3(a.lam_x, n, s->map_d, gx_0, s->stream));
+  NB_CUDA(launch_pack_vec3(a.lam_v, n, s->map_d, gv_0, s->stream));
+  return NB_OK;
+}
+
+int nb_sim_adjoint_backward(nb_sim* s, const float* gx_T, const float* gv_T, float* gx_0,
+                            float* gv_0) {
+  if (!s || !gx_T || !gx_0 || !gv_0) return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard dg_(s->device);
+  AdjointState& a = s->adj;
+  if (!a.valid) return set_error(NB_ERR_STATE, "call nb_sim_adjoint_forward first");
+  NB_TRY(ensure_staging(s));
+  const size_t n = s->n_real;
+  float* stage = s->staging_d;  // 7n floats: the two n x 3 arrays in and out
+  NB_CUDA(cudaMemcpyAsync(stage, gx_T, 3 * n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  if (gv_T)
+    NB_CUDA(cudaMemcpyAsync(stage + 3 * n, gv_T, 3 * n * sizeof(float), cudaMemcpyHostToDevice,
+                            s->stream));
+  NB_TRY(adjoint_backward_stream(s, stage, gv_T ? stage + 3 * n : nullptr, stage, stage + 3 * n));
   NB_CUDA(cudaMemcpyAsync(gx_0, stage, 3 * n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
-  NB_CUDA(launch_pack_vec3(a.lam_v, n, s->map_d, stage + 3 * n, s->stream));
   NB_CUDA(cudaMemcpyAsync(gv_0, stage + 3 * n, 3 * n * sizeof(float), cudaMemcpyDeviceToHost,
                           s->stream));
   NB_CUDA(cudaStreamSynchronize(s->stream));
   return check_error_word(s);
+}
+
+int nb_sim_adjoint_backward_device(nb_sim* s, const float* gx_T_device, const float* gv_T_device,
+                                   float* gx_0_device, float* gv_0_device) {
+  if (!s || !gx_T_device || !gx_0_device || !gv_0_device)
+    return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard dg_(s->device);
+  if (!s->adj.valid) return set_error(NB_ERR_STATE, "call nb_sim_adjoint_forward first");
+  return adjoint_backward_stream(s, gx_T_device, gv_T_device, gx_0_device, gv_0_device);
 }
 
 }  // extern "C"

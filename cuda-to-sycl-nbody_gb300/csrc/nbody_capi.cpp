@@ -240,19 +240,29 @@ static int build_main_worklist(nb_sim* s, int cfg) {
   return NB_OK;
 }
 
-static int build_per_system_worklists(nb_sim* s) {
-  if (s->wl_sys_cfg == s->cfg && s->wl_sys.size() == s->sys_h.size()) return NB_OK;
+static int default_config_for(nb_sim* s, int32_t first, int32_t count);
+
+// One work list per system for the one-launch-per-system baseline.  Policy
+// kPerSystemOwnShape plans each system with the shape it would get as a
+// simulation of its own (default_config_for), the way a caller launching each
+// system separately would; kPerSystemSimShape gives every system the simulation's
+// current shape.
+static int build_per_system_worklists(nb_sim* s, int policy) {
+  const int key = policy == kPerSystemOwnShape ? -2 : s->cfg;
+  if (s->wl_sys_cfg == key && s->wl_sys.size() == s->sys_h.size()) return NB_OK;
   for (auto& w : s->wl_sys) free_worklist(w);
   s->wl_sys.clear();
-  const KernelShape sh = force_config_shape(s->cfg);
-  const int mg = max_grid_for(s, s->cfg);
+  s->wl_sys_cfg = -1;
   for (int32_t k = 0; k < static_cast<int32_t>(s->sys_h.size()); ++k) {
-    const WorkListHost h = plan_worklist(s->sys_h.data(), k, 1, sh.bi(), sh.bj, mg);
+    const int cfg = policy == kPerSystemOwnShape ? default_config_for(s, k, 1) : s->cfg;
+    const KernelShape sh = force_config_shape(cfg);
+    const WorkListHost h = plan_worklist(s->sys_h.data(), k, 1, sh.bi(), sh.bj,
+                                         max_grid_for(s, cfg));
     WorkListDev w;
-    NB_TRY(upload_worklist(s, h, s->cfg, &w));
+    NB_TRY(upload_worklist(s, h, cfg, &w));
     s->wl_sys.push_back(w);
   }
-  s->wl_sys_cfg = s->cfg;
+  s->wl_sys_cfg = key;
   return NB_OK;
 }
 
@@ -341,8 +351,8 @@ int launch_with(nb_sim* s, ForceArgs a, const WorkListDev& w) {
 }
 
 // One force evaluation: integrate into the other buffer (accel_out == nullptr)
-// or write accelerations.  `per_system` issues one launch per system.
-int force_pass(nb_sim* s, float4* accel_out, bool per_system) {
+// or write accelerations.  `per_system` (kPerSystem*) issues one launch per system.
+int force_pass(nb_sim* s, float4* accel_out, int per_system) {
   ForceArgs a = base_args(s);
   a.accel_out = accel_out;
   if (s->params.calc_method == NB_PREDICATED) {
@@ -357,7 +367,7 @@ int force_pass(nb_sim* s, float4* accel_out, bool per_system) {
       NB_TRY(launch_reference_order_range(s, a, 0, nsys));
     }
   } else if (per_system) {
-    NB_TRY(build_per_system_worklists(s));
+    NB_TRY(build_per_system_worklists(s, per_system));
     for (const auto& w : s->wl_sys) NB_TRY(launch_with(s, a, w));
   } else {
     NB_TRY(launch_with(s, a, s->wl));
@@ -389,18 +399,24 @@ int check_error_word(nb_sim* s) {
 // autotuner may pick otherwise, and shapes round differently).  Measured against
 // the autotuner's pick: N = 25,600 -> 256 x 2 x 256 (0.24 ms, the 1M shape takes
 // 0.32), 65,536 -> 256 x 4 x 1024, 262,144 and 1M -> 256 x 4 x 2048.
-static int default_config(nb_sim* s) {
+// default_config_for judges systems [first, first + count) alone.
+static int default_config_for(nb_sim* s, int32_t first, int32_t count) {
   static const int kCandidates[] = {9, 8, 10, 3, 4};  // largest tiles first
   for (const int cfg : kCandidates) {
     const KernelShape sh = force_config_shape(cfg);
     int64_t blocks = 0;
-    for (const auto& d : s->sys_h) {
+    for (int32_t k = first; k < first + count; ++k) {
+      const SystemDesc& d = s->sys_h[k];
       const int64_t i_tiles = (d.n + sh.bi() - 1) / sh.bi();
       blocks += i_tiles * ((d.npad + sh.bj - 1) / sh.bj);
     }
     if (blocks >= 16 * static_cast<int64_t>(max_grid_for(s, cfg))) return cfg;
   }
   return 4;
+}
+
+static int default_config(nb_sim* s) {
+  return default_config_for(s, 0, static_cast<int32_t>(s->sys_h.size()));
 }
 
 static int create_impl(const nb_params* p, uint32_t num_systems, const uint32_t* sizes,
@@ -681,7 +697,7 @@ int nb_sim_advance(nb_sim* s, int32_t iterations) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
   DeviceGuard dg_(s->device);
   if (iterations < 0) return set_error(NB_ERR_INVALID_ARGUMENT, "iterations < 0");
-  for (int32_t k = 0; k < iterations; ++k) NB_TRY(force_pass(s, nullptr, false));
+  for (int32_t k = 0; k < iterations; ++k) NB_TRY(force_pass(s, nullptr, kPerSystemNone));
   return NB_OK;
 }
 
@@ -689,7 +705,8 @@ int nb_sim_advance_per_system(nb_sim* s, int32_t iterations) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
   DeviceGuard dg_(s->device);
   if (iterations < 0) return set_error(NB_ERR_INVALID_ARGUMENT, "iterations < 0");
-  for (int32_t k = 0; k < iterations; ++k) NB_TRY(force_pass(s, nullptr, true));
+  for (int32_t k = 0; k < iterations; ++k)
+    NB_TRY(force_pass(s, nullptr, kPerSystemOwnShape));
   return NB_OK;
 }
 
@@ -710,9 +727,14 @@ int nb_sim_time_iterations(nb_sim* s, int32_t iterations, int32_t per_system, fl
   if (!s || !ms) return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
   DeviceGuard dg_(s->device);
   if (iterations < 0) return set_error(NB_ERR_INVALID_ARGUMENT, "iterations < 0");
-  if (per_system) NB_TRY(build_per_system_worklists(s));
+  if (per_system != kPerSystemNone && per_system != kPerSystemOwnShape &&
+      per_system != kPerSystemSimShape)
+    return set_error(NB_ERR_INVALID_ARGUMENT, "per_system must be 0, 1 or 2");
+  if (per_system && s->params.calc_method == NB_BRANCH &&
+      s->params.accumulator != NB_ACC_REFERENCE_ORDER)
+    NB_TRY(build_per_system_worklists(s, per_system));
   NB_CUDA(cudaEventRecord(s->ev0, s->stream));
-  for (int32_t k = 0; k < iterations; ++k) NB_TRY(force_pass(s, nullptr, per_system != 0));
+  for (int32_t k = 0; k < iterations; ++k) NB_TRY(force_pass(s, nullptr, per_system));
   NB_CUDA(cudaEventRecord(s->ev1, s->stream));
   NB_CUDA(cudaEventSynchronize(s->ev1));
   NB_CUDA(cudaEventElapsedTime(ms, s->ev0, s->ev1));
@@ -773,7 +795,7 @@ int nb_sim_accelerations(nb_sim* s, float* ax, float* ay, float* az) {
   DeviceGuard dg_(s->device);
   NB_TRY(ensure_accel(s));
   NB_TRY(ensure_staging(s));
-  NB_TRY(force_pass(s, s->acc_d, false));
+  NB_TRY(force_pass(s, s->acc_d, kPerSystemNone));
   const size_t n = s->n_real;
   NB_CUDA(launch_pack_accel(s->acc_d, n, s->map_d, s->staging_d, s->stream));
   float* outs[3] = {ax, ay, az};
@@ -890,9 +912,9 @@ int nb_sim_autotune(nb_sim* s, int32_t* chosen) {
     for (int k = 0; k < reference_order_num_shapes(); ++k) {
       s->ro_shape = k;
       NB_TRY(build_reference_order_tiles(s));
-      NB_TRY(force_pass(s, s->acc_d, false));  // warm-up
+      NB_TRY(force_pass(s, s->acc_d, kPerSystemNone));  // warm-up
       NB_CUDA(cudaEventRecord(s->ev0, s->stream));
-      NB_TRY(force_pass(s, s->acc_d, false));
+      NB_TRY(force_pass(s, s->acc_d, kPerSystemNone));
       NB_CUDA(cudaEventRecord(s->ev1, s->stream));
       NB_CUDA(cudaEventSynchronize(s->ev1));
       float ms = 0.f;
@@ -912,9 +934,9 @@ int nb_sim_autotune(nb_sim* s, int32_t* chosen) {
   for (int c = 0; c < num_force_configs(); ++c) {
     NB_TRY(build_main_worklist(s, c));
     s->cfg = c;
-    NB_TRY(force_pass(s, s->acc_d, false));  // warm-up
+    NB_TRY(force_pass(s, s->acc_d, kPerSystemNone));  // warm-up
     NB_CUDA(cudaEventRecord(s->ev0, s->stream));
-    NB_TRY(force_pass(s, s->acc_d, false));
+    NB_TRY(force_pass(s, s->acc_d, kPerSystemNone));
     NB_CUDA(cudaEventRecord(s->ev1, s->stream));
     NB_CUDA(cudaEventSynchronize(s->ev1));
     float ms = 0.f;
@@ -922,7 +944,7 @@ int nb_sim_autotune(nb_sim* s, int32_t* chosen) {
     int reps = ms < 2.f ? 5 : (ms < 50.f ? 2 : 0);
     if (reps > 0) {
       NB_CUDA(cudaEventRecord(s->ev0, s->stream));
-      for (int r = 0; r < reps; ++r) NB_TRY(force_pass(s, s->acc_d, false));
+      for (int r = 0; r < reps; ++r) NB_TRY(force_pass(s, s->acc_d, kPerSystemNone));
       NB_CUDA(cudaEventRecord(s->ev1, s->stream));
       NB_CUDA(cudaEventSynchronize(s->ev1));
       NB_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
@@ -1054,7 +1076,7 @@ int nb_sim_graph_capture(nb_sim* s, int32_t iterations) {
       return cuda_error(e, "cudaStreamBeginCapture");
     }
     int st = NB_OK;
-    for (int32_t k = 0; k < iterations && st == NB_OK; ++k) st = force_pass(s, nullptr, false);
+    for (int32_t k = 0; k < iterations && st == NB_OK; ++k) st = force_pass(s, nullptr, kPerSystemNone);
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(s->stream, &g);
     s->cur = cur0;  // nothing ran

@@ -136,6 +136,7 @@ SIGNATURES = {
     "nb_sim_fp64_accelerations": (C.c_int, [_P, _U64, C.c_uint64, _D, _D, _D]),
     "nb_sim_adjoint_forward": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "nb_sim_adjoint_backward": (C.c_int, [_P] + [_F] * 4),
+    "nb_sim_adjoint_backward_device": (C.c_int, [_P] * 5),
     "nb_accelerations_noalloc": (C.c_int, [_P, C.c_uint64, C.c_float, C.c_float, _P, _P]),
     "nb_ic_thin_disk": (C.c_int, [C.c_uint64, C.c_uint64, C.c_float] + [_F] * 7),
     "nb_ic_plummer": (C.c_int, [C.c_uint64, C.c_uint64] + [_F] * 7),
@@ -404,7 +405,11 @@ class Simulation:
         """Failure-detection test hook: the next launch's bounded waits run out."""
         _check(lib.nb_sim_inject_wait_timeout(self._h))
 
-    def time_iterations(self, iterations: int, per_system: bool = False) -> float:
+    def time_iterations(self, iterations: int, per_system: int = 0) -> float:
+        """Device milliseconds of `iterations` iterations (CUDA events).  per_system:
+        0 one launch over every system; 1 (or True) one launch per system with the
+        shape each would get alone; 2 one launch per system with this simulation's
+        shape."""
         ms = C.c_float()
         _check(lib.nb_sim_time_iterations(self._h, iterations, int(per_system), C.byref(ms)))
         return ms.value
@@ -523,6 +528,14 @@ class Simulation:
         ov = np.empty(3 * self.n, dtype=np.float32)
         _check(lib.nb_sim_adjoint_backward(self._h, _fp(gx), _fp(gv), _fp(ox), _fp(ov)))
         return ox.reshape(self.n, 3), ov.reshape(self.n, 3)
+
+    def adjoint_backward_device(self, gx_T_ptr: int, gv_T_ptr: int | None, gx_0_ptr: int,
+                                gv_0_ptr: int) -> None:
+        """nb_sim_adjoint_backward on device arrays (n x 3 float32 each), enqueued on
+        the simulation's stream."""
+        _check(lib.nb_sim_adjoint_backward_device(
+            self._h, C.c_void_p(gx_T_ptr), C.c_void_p(gv_T_ptr) if gv_T_ptr else None,
+            C.c_void_p(gx_0_ptr), C.c_void_p(gv_0_ptr)))
 
 
 class DiskGalaxySimulator:

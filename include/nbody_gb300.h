@@ -174,7 +174,10 @@ int nb_sim_step(nb_sim* s);
 /* Enqueue `iterations` iterations on the simulation's stream; returns without
  * waiting. */
 int nb_sim_advance(nb_sim* s, int32_t iterations);
-/* Baseline for ensembles: the same iterations issued as one launch per system. */
+/* Baseline for ensembles: the same iterations issued as one launch per system,
+ * the way the reference's stepSim launches one grid for its one system
+ * (simulator.cu:49-63).  Each system's launch is planned with the kernel shape it
+ * would get as a simulation of its own. */
 int nb_sim_advance_per_system(nb_sim* s, int32_t iterations);
 /* Failure-detection test hook (one shot): the next force launch leaves the
  * first shared-memory tile of every CTA uncopied, so each CTA's bounded wait
@@ -191,7 +194,10 @@ int nb_inject_alloc_failure(int32_t nth);
 /* Wait for the stream and report any device-side error (e.g. a wait that timed out). */
 int nb_sim_synchronize(nb_sim* s);
 /* Run `iterations` iterations bracketed by CUDA events on the simulation's stream
- * and return the device time in milliseconds. */
+ * and return the device time in milliseconds.  per_system: 0 = one launch over
+ * every system; 1 = one launch per system, each with the kernel shape it would get
+ * alone (as nb_sim_advance_per_system); 2 = one launch per system, all with the
+ * simulation's current shape. */
 int nb_sim_time_iterations(nb_sim* s, int32_t iterations, int32_t per_system, float* ms);
 
 /* recvFromDevice (simulator.cu:106-129).  Any output pointer may be NULL. */
@@ -279,6 +285,12 @@ int nb_sim_adjoint_forward(nb_sim* s, int32_t T, int32_t checkpoint_every);
  * checkpoints; leaves the simulation at its state after the forward run. */
 int nb_sim_adjoint_backward(nb_sim* s, const float* gx_T, const float* gv_T,
                             float* gx_0, float* gv_0);
+/* nb_sim_adjoint_backward on device arrays (n x 3 floats each, xyz-interleaved;
+ * gv_T_device may be NULL), enqueued on the simulation's stream without waiting:
+ * for callers whose loss and optimiser live on the GPU. */
+int nb_sim_adjoint_backward_device(nb_sim* s, const float* gx_T_device,
+                                   const float* gv_T_device, float* gx_0_device,
+                                   float* gv_0_device);
 
 /* ---- accelerations without allocation ------------------------------------------ */
 /* For callers that cannot allocate GPU memory themselves or through this library

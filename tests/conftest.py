@@ -19,6 +19,9 @@ for p in (ROOT / "cuda-to-sycl-nbody_gb300", ROOT / "tests"):
 
 
 def pytest_configure(config):
+    # Temporary files of the tests stay inside the repository (git-ignored).
+    if not config.option.basetemp:
+        config.option.basetemp = str(ROOT / ".pytest_tmp")
     config.addinivalue_line("markers", "gpu: needs a GB300 (sm_103a) GPU")
     config.addinivalue_line("markers", "slow: full-size workload (seconds of GPU time)")
     subprocess.run([sys.executable, str(ROOT / "cuda-to-sycl-nbody_gb300" / "build.py")],

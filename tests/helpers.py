@@ -38,3 +38,20 @@ def params(n: int, G=1.0, dt=1e-3, damping=0.999, eps=1e-3, method=nb.BRANCH,
 def g_eff(G: float, m: float) -> float:
     """G * m rounded as the library folds an equal mass into G (float32)."""
     return float(np.float32(G) * np.float32(m))
+
+
+def displacement_errors(got, ref, start):
+    """Position errors relative to how far the particles moved: (RMS of |x_got -
+    x_ref| over the RMS of |x_ref - x_start|, max per-particle |x_got - x_ref| over
+    that particle's |x_ref - x_start| floored at 10% of the RMS displacement).
+    Positions are [x, y, z] arrays."""
+    g = np.stack([np.asarray(a, dtype=np.float64) for a in got])
+    r = np.stack([np.asarray(a, dtype=np.float64) for a in ref])
+    s = np.stack([np.asarray(a, dtype=np.float64) for a in start])
+    d = np.linalg.norm(g - r, axis=0)
+    disp = np.linalg.norm(r - s, axis=0)
+    rms_disp = float(np.sqrt(np.mean(disp ** 2)))
+    if rms_disp == 0.0:
+        return float(np.max(d)), float(np.max(d))
+    return (float(np.sqrt(np.mean(d ** 2)) / rms_disp),
+            float(np.max(d / np.maximum(disp, 0.1 * rms_disp))))

@@ -13,6 +13,7 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent.parent
 ORACLE_LIB = ROOT / "oracle" / "liboracle.so"
+PORT_LIB = ROOT / "oracle" / "libcpu_port.so"
 REF_DIR = ROOT / "oracle" / "_ref"
 REF_CUBIN = REF_DIR / "simulator_sm103a.cubin"
 REF_RUNNER = REF_DIR / "libref_runner.so"
@@ -47,8 +48,59 @@ def lib() -> C.CDLL:
         L.oracle_render.argtypes = [C.c_int64] + [_F] * 7 + [C.c_int, C.c_int, _F, _F, C.c_int,
                                                               _F, C.c_int, _F]
         L.oracle_render.restype = C.c_int
+        L.workload_plummer.argtypes = [C.c_uint64, C.c_uint64] + [_F] * 7
+        L.workload_plummer.restype = C.c_int
         _lib = L
     return _lib
+
+
+_port = None
+
+
+def port() -> C.CDLL:
+    """The timed CPU port (oracle/cpu_port.c, built -O3 -ffast-math -fopenmp)."""
+    global _port
+    if _port is None:
+        if not PORT_LIB.exists():
+            raise RuntimeError(f"{PORT_LIB} missing: run `make -C oracle`")
+        L = C.CDLL(str(PORT_LIB))
+        L.cpu_port_accel.argtypes = [C.c_int64] + [_F] * 3 + [C.c_float, C.c_float, _I64,
+                                                              C.c_int64] + [_F] * 3
+        L.cpu_port_accel.restype = None
+        L.cpu_port_num_threads.restype = C.c_int
+        L.cpu_port_set_num_threads.argtypes = [C.c_int]
+        L.cpu_port_set_num_threads.restype = None
+        _port = L
+    return _port
+
+
+def port_accel(pos, G, eps, rows=None):
+    """G times the force sum of `rows` (all when None), unit masses, by the timed port."""
+    x, y, z = (_f(a) for a in pos)
+    r = None if rows is None else np.ascontiguousarray(rows, dtype=np.int64)
+    cnt = x.size if r is None else r.size
+    out = [np.empty(cnt, dtype=np.float32) for _ in range(3)]
+    port().cpu_port_accel(x.size, _p(x), _p(y), _p(z), G, eps,
+                          None if r is None else r.ctypes.data_as(_I64),
+                          -1 if r is None else r.size, *[_p(o) for o in out])
+    return out
+
+
+def port_set_num_threads(n: int) -> None:
+    port().cpu_port_set_num_threads(int(n))
+
+
+def port_num_threads() -> int:
+    return port().cpu_port_num_threads()
+
+
+def plummer(seed: int, n: int):
+    """The workload's seeded Plummer sphere (oracle/workload_ic.c):
+    ([x, y, z], [vx, vy, vz], mass), float32."""
+    o = [np.empty(n, dtype=np.float32) for _ in range(7)]
+    if lib().workload_plummer(seed, n, *[_p(a) for a in o]) != 0:
+        raise MemoryError("workload_plummer")
+    return o[:3], o[3:6], o[6]
 
 
 def _f(a) -> np.ndarray:

@@ -146,3 +146,30 @@ def test_adjoint_per_pair_masses():
     ((xT * torch.from_numpy(gxT)).sum() + (vT * torch.from_numpy(gvT)).sum()).backward()
     for g, r in ((gx, x.grad.numpy()), (gv, v.grad.numpy())):
         assert np.linalg.norm(g - r) / np.linalg.norm(r) <= 1e-4
+
+
+def test_adjoint_device_entry_point_matches_host_entry_point():
+    # nb_sim_adjoint_backward_device: the same sweep on device arrays, stream-ordered.
+    n, steps = 1000, 12
+    pos, vel, _ = disk_case(n, seed=17)
+    m = (np.random.default_rng(6).uniform(0.5, 1.5, n) / n).astype(np.float32)
+    rng = np.random.default_rng(7)
+    gxT = rng.normal(size=3 * n).astype(np.float32)
+    gvT = rng.normal(size=3 * n).astype(np.float32)
+    with nb.Simulation(params(n, G=G, dt=DT, damping=DAMP), pos, vel, m) as sim:
+        sim.adjoint_forward(steps, 5)
+        host = sim.adjoint_backward(gxT, gvT)
+        host_nov = sim.adjoint_backward(gxT)
+        dev_in = [torch.from_numpy(a).cuda() for a in (gxT, gvT)]
+        out = [torch.full((3 * n,), float("nan"), device="cuda") for _ in range(2)]
+        torch.cuda.synchronize()
+        sim.adjoint_backward_device(dev_in[0].data_ptr(), dev_in[1].data_ptr(),
+                                    out[0].data_ptr(), out[1].data_ptr())
+        sim.synchronize()
+        dev = [o.cpu().numpy().reshape(n, 3) for o in out]
+        sim.adjoint_backward_device(dev_in[0].data_ptr(), None, out[0].data_ptr(),
+                                    out[1].data_ptr())
+        sim.synchronize()
+        dev_nov = [o.cpu().numpy().reshape(n, 3) for o in out]
+    for a, b in zip(host + host_nov, dev + dev_nov):
+        assert np.array_equal(a, b)

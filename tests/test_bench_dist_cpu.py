@@ -62,10 +62,23 @@ def test_reference_arm_json_contract():
     import json
     import subprocess
 
-    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference",
-                        "--steps", "1", "--warmup", "3", "--cpu-seconds", "0.5"],
-                       capture_output=True, text=True, timeout=600, cwd=str(ROOT))
+    # Run the arm in a process that afterwards reports whether the library under
+    # test was ever mapped: the reference arm must not load it.
+    script = (
+        "import runpy, sys\n"
+        "sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '3',\n"
+        "            '--cpu-seconds', '0.5']\n"
+        "try:\n"
+        "    runpy.run_path('bench.py', run_name='__main__')\n"
+        "except SystemExit as e:\n"
+        "    assert not e.code, e.code\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print('LIBRARY_MAPPED' if 'libnbody_gb300' in maps else 'LIBRARY_NOT_MAPPED',\n"
+        "      file=sys.stderr)\n")
+    r = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True,
+                       timeout=600, cwd=str(ROOT))
     assert r.returncode == 0, r.stderr[-2000:]
+    assert "LIBRARY_NOT_MAPPED" in r.stderr, r.stderr[-2000:]
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference"
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",

@@ -82,3 +82,29 @@ def test_energy_of_small_systems(n):
             pe -= mm[i] * mm[j] / np.sqrt(np.sum((x[i] - x[j]) ** 2) + 1e-3)
     assert np.isclose(e["kinetic"], ke, rtol=1e-12) and np.isclose(e["potential"], pe, rtol=1e-12,
                                                                      atol=1e-300)
+
+
+def test_timed_cpu_port_agrees_with_oracle():
+    # oracle/cpu_port.c: the same kernel body built -O3 -ffast-math for the timed
+    # baseline; reordered sums (and possibly an rsqrt estimate) stay within 1e-4.
+    pos, _, m = disk_case(3000, seed=5)
+    G = float(np.float32(m[0]))
+    rows = np.arange(0, 3000, 7)
+    got = orc.port_accel(pos, G, 1e-3, rows=rows)
+    ref = orc.accel_fp32(pos, None, G, 1e-3, rows=rows)
+    rms, mx = vec_errors(got, ref)
+    assert rms <= 1e-4 and mx <= 1e-4, (rms, mx)
+    both = orc.port_accel(pos, G, 0.0, rows=np.array([0, 1]))   # eps = 0: j == i left out
+    assert all(np.all(np.isfinite(a)) for a in both)
+
+
+@pytest.mark.parametrize("seed,n", [(20261203, 4096), (7, 1), (11, 333)])
+def test_workload_plummer_is_the_library_generator_bit_for_bit(seed, n):
+    # The benchmark's reference arm makes its Plummer inputs with the oracle's
+    # restatement (it never loads the library); both must give the same floats.
+    import nbody_gb300 as nb
+
+    a = orc.plummer(seed, n)
+    b = nb.plummer(seed, n)
+    for u, v in zip(list(a[0]) + list(a[1]) + [a[2]], list(b[0]) + list(b[1]) + [b[2]]):
+        assert np.array_equal(u, v)
