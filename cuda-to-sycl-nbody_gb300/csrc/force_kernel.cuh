@@ -255,7 +255,8 @@ __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
   for (int sgi = seg_lo; sgi < seg_hi; ++sgi) {
     const Segment sg = a.segs[sgi];
     const SystemDesc sd = a.sys[sg.sys];
-    const int ibase = sg.itile * BI;
+    const int ibase = sd.shard_first + sg.itile * BI;
+    const int iend = shard_end(sd);
 
     float2 nx[R], ny[R], nz[R], ax[R], ay[R], az[R];
     float2 sx[R], sy[R], sz[R], cx[R], cy[R], cz[R];  // compensated running sums
@@ -263,7 +264,7 @@ __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int li = ibase + r * THREADS + tid;
-      const int lc = li < sd.n ? li : sd.n - 1;
+      const int lc = li < iend ? li : iend - 1;
       gi[r] = sd.offset + lc;
       const float xi = a.pos[pair_index(gi[r], 0)];
       const float yi = a.pos[pair_index(gi[r], 1)];
@@ -329,7 +330,7 @@ __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int li = ibase + r * THREADS + tid;
-        if (li < sd.n)
+        if (li < iend)
           finish_particle(a, sd, gi[r], hx[r] + lx[r], hy[r] + ly[r], hz[r] + lz[r], -nx[r].x,
                           -ny[r].x, -nz[r].x);
       }
@@ -361,7 +362,7 @@ __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
       for (int r = 0; r < R; ++r) {
         const int idx = r * THREADS + tid;
         const int li = ibase + idx;
-        if (li >= sd.n) continue;
+        if (li >= iend) continue;
         float tx = 0.f, ty = 0.f, tz = 0.f;      // running totals
         float ex = 0.f, ey = 0.f, ez = 0.f;      // compensation (compensated mode)
         float qx = 0.f, qy = 0.f, qz = 0.f;      // sum of the parts' low words

@@ -39,8 +39,18 @@ struct SystemDesc {
   float gscale;    // G (per-pair masses) or G * m (equal masses, m folded out of the pair loop)
   float mass;      // the common mass when the system is equal-mass, else 0
   int32_t equal_mass;
+  // The particles a force pass integrates (a shard, nb_sim_set_shard): i in
+  // [shard_first, shard_first + shard_count), each against all n; shard_count 0
+  // means to the end of the system.  shard_first is a multiple of kPadQuantum.
+  int32_t shard_first;
+  int32_t shard_count;
   int32_t pad_;
 };
+
+// One past the last i-particle a force pass integrates in system `d`.
+__host__ __device__ inline int32_t shard_end(const SystemDesc& d) {
+  return d.shard_count ? d.shard_first + d.shard_count : d.n;
+}
 
 // One entry of a CTA's work list: i-tile `itile` of system `sys` against j-tiles
 // [jt0, jt1).  `fix` >= 0 when the i-tile's j-range is split over several CTAs:

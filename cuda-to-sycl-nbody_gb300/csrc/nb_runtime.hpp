@@ -17,6 +17,8 @@
 
 namespace nbg {
 
+// A work list on the device.  cfg >= 0: a shape of the tuned force kernel;
+// cfg < 0: reference-order shape -1 - cfg.
 struct WorkListDev {
   int32_t cfg = -1;
   int32_t grid = 0;
@@ -81,18 +83,18 @@ struct nb_sim {
   int cfg = 0;
   nbg::WorkListDev wl;
   std::vector<nbg::WorkListDev> wl_sys;
-  int wl_sys_cfg = -1;  // shape of wl_sys (-2: each system's own default shape)
+  int wl_sys_policy = -1;  // how wl_sys was planned (kPerSystem*), -1: not yet
+  int wl_sys_cfg = 0;      // and with which shape, for kPerSystemSimShape
   float4* partials_d = nullptr;
   size_t partials_cap = 0;
   int32_t* counters_d = nullptr;
   size_t counters_cap = 0;
 
-  // NB_ACC_REFERENCE_ORDER: the reference-order kernel's shape, its (system, i-tile)
-  // pairs, the first tile of each system (systems + 1 entries) and its grid.
+  // NB_ACC_REFERENCE_ORDER: the reference-order kernel's shape, its work list
+  // (config index -1 - shape) and the duplicated j-layout of the positions.
   int ro_shape = 0;
-  int32_t* ro_tiles_d = nullptr;
-  std::vector<int32_t> ro_first;
-  int ro_grid = 0;
+  nbg::WorkListDev ro_wl;
+  float4* ro_dup_d = nullptr;  // [2 * n_pad]
 
   cudaEvent_t ev0 = nullptr;
   cudaEvent_t ev1 = nullptr;

@@ -178,6 +178,9 @@ int nb_sim_adjoint_forward(nb_sim* s, int32_t T, int32_t checkpoint_every) {
     return set_error(NB_ERR_INVALID_ARGUMENT, "T and checkpoint_every must be >= 1");
   if (s->params.calc_method != NB_BRANCH)
     return set_error(NB_ERR_STATE, "the adjoint is defined for the BRANCH method only");
+  for (const SystemDesc& d : s->sys_h)
+    if (d.shard_first != 0 || d.shard_count != 0)
+      return set_error(NB_ERR_STATE, "the adjoint needs the whole system, not a shard");
   const int32_t every = std::min(checkpoint_every, T);
   const int32_t ncp = (T + every - 1) / every;
   s->adj.valid = false;

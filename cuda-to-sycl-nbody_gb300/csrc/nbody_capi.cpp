@@ -165,10 +165,31 @@ static int upload_state(nb_sim* s, const float* const arrays[7], bool with_mass)
   return NB_OK;
 }
 
+// Captured graphs bake in the work lists' and the scratch's device addresses:
+// whenever either is replaced, the graphs go too (nb_sim_graph_launch then reports
+// that none is captured).
+static void drop_graphs(nb_sim* s) {
+  for (int b = 0; b < 2; ++b) {
+    if (s->gexec[b]) cudaGraphExecDestroy(s->gexec[b]);
+    if (s->graph[b]) cudaGraphDestroy(s->graph[b]);
+    s->gexec[b] = nullptr;
+    s->graph[b] = nullptr;
+  }
+  s->graph_iters = 0;
+}
+
+// Shape of work-list config `cfg` (>= 0: tuned kernel; < 0: reference order).
+static KernelShape shape_of(int cfg) {
+  return cfg >= 0 ? force_config_shape(cfg) : reference_order_shape(-1 - cfg);
+}
+
 static int ensure_scratch(nb_sim* s, const WorkListDev& w) {
-  const KernelShape sh = force_config_shape(w.cfg);
-  const size_t rec = (s->params.accumulator == NB_ACC_COMPENSATED) ? 2 : 1;
+  const KernelShape sh = shape_of(w.cfg);
+  // Partial sums: (hi, lo) records for the compensated tuned kernel, one record
+  // otherwise (the reference-order kernel's hand-over holds one float4 per particle).
+  const size_t rec = (w.cfg >= 0 && s->params.accumulator == NB_ACC_COMPENSATED) ? 2 : 1;
   const size_t need = static_cast<size_t>(w.slots) * sh.bi() * rec;
+  if (need > s->partials_cap || static_cast<size_t>(w.nfix) > s->counters_cap) drop_graphs(s);
   if (need > s->partials_cap) {
     dev_free(s->partials_d);
     NB_TRY(dev_alloc(&s->partials_d, need));
@@ -186,8 +207,10 @@ static int ensure_scratch(nb_sim* s, const WorkListDev& w) {
 static int max_grid_for(nb_sim* s, int cfg) {
   int blocks = 0;
   const bool comp = s->params.accumulator == NB_ACC_COMPENSATED;
-  if (force_blocks_per_sm(cfg, comp, s->per_pair_mass, &blocks) != cudaSuccess || blocks < 1)
-    blocks = 1;
+  const cudaError_t e = cfg >= 0
+                            ? force_blocks_per_sm(cfg, comp, s->per_pair_mass, &blocks)
+                            : reference_order_blocks_per_sm(-1 - cfg, &blocks);
+  if (e != cudaSuccess || blocks < 1) blocks = 1;
   return blocks * s->sms;
 }
 
@@ -235,89 +258,69 @@ static int build_main_worklist(nb_sim* s, int cfg) {
                                        sh.bi(), sh.bj, max_grid_for(s, cfg));
   WorkListDev w;
   NB_TRY(upload_worklist(s, h, cfg, &w));
+  drop_graphs(s);
   free_worklist(s->wl);
   s->wl = w;
   return NB_OK;
 }
 
 static int default_config_for(nb_sim* s, int32_t first, int32_t count);
+static int default_reference_order_for(nb_sim* s, int32_t first, int32_t count);
+
+static bool reference_order_mode(const nb_sim* s) {
+  return s->params.calc_method == NB_BRANCH && s->params.accumulator == NB_ACC_REFERENCE_ORDER;
+}
+
+// (Re)build the reference-order work list for shape `shape` (all systems).
+static int reference_order_grid(nb_sim* s, int shape, int32_t first, int32_t count);
+
+static int build_reference_order_worklist(nb_sim* s, int shape) {
+  const int cfg = -1 - shape;
+  const KernelShape sh = reference_order_shape(shape);
+  const int32_t nsys = static_cast<int32_t>(s->sys_h.size());
+  const WorkListHost h = plan_worklist(s->sys_h.data(), 0, nsys, sh.bi(), sh.bj,
+                                       reference_order_grid(s, shape, 0, nsys));
+  WorkListDev w;
+  NB_TRY(upload_worklist(s, h, cfg, &w));
+  drop_graphs(s);
+  free_worklist(s->ro_wl);
+  s->ro_wl = w;
+  return NB_OK;
+}
 
 // One work list per system for the one-launch-per-system baseline.  Policy
 // kPerSystemOwnShape plans each system with the shape it would get as a
-// simulation of its own (default_config_for), the way a caller launching each
-// system separately would; kPerSystemSimShape gives every system the simulation's
-// current shape.
+// simulation of its own (default_config_for / default_reference_order_for), the
+// way a caller launching each system separately would; kPerSystemSimShape gives
+// every system the simulation's current shape.
 static int build_per_system_worklists(nb_sim* s, int policy) {
-  const int key = policy == kPerSystemOwnShape ? -2 : s->cfg;
-  if (s->wl_sys_cfg == key && s->wl_sys.size() == s->sys_h.size()) return NB_OK;
+  const bool ro = reference_order_mode(s);
+  const int sim_cfg = ro ? -1 - s->ro_shape : s->cfg;
+  if (s->wl_sys_policy == policy && (policy == kPerSystemOwnShape || s->wl_sys_cfg == sim_cfg) &&
+      s->wl_sys.size() == s->sys_h.size())
+    return NB_OK;
   for (auto& w : s->wl_sys) free_worklist(w);
   s->wl_sys.clear();
-  s->wl_sys_cfg = -1;
+  s->wl_sys_policy = -1;
   for (int32_t k = 0; k < static_cast<int32_t>(s->sys_h.size()); ++k) {
-    const int cfg = policy == kPerSystemOwnShape ? default_config_for(s, k, 1) : s->cfg;
-    const KernelShape sh = force_config_shape(cfg);
-    const WorkListHost h = plan_worklist(s->sys_h.data(), k, 1, sh.bi(), sh.bj,
-                                         max_grid_for(s, cfg));
+    int cfg = sim_cfg;
+    if (policy == kPerSystemOwnShape)
+      cfg = ro ? -1 - default_reference_order_for(s, k, 1) : default_config_for(s, k, 1);
+    const KernelShape sh = shape_of(cfg);
+    const int grid = cfg >= 0 ? max_grid_for(s, cfg) : reference_order_grid(s, -1 - cfg, k, 1);
+    const WorkListHost h = plan_worklist(s->sys_h.data(), k, 1, sh.bi(), sh.bj, grid);
     WorkListDev w;
     NB_TRY(upload_worklist(s, h, cfg, &w));
     s->wl_sys.push_back(w);
   }
-  s->wl_sys_cfg = key;
+  s->wl_sys_policy = policy;
+  s->wl_sys_cfg = sim_cfg;
   return NB_OK;
 }
 
-// i-tiles of all systems for reference-order shape `shape`.
-static int32_t reference_order_tile_count(const nb_sim* s, int shape) {
-  const int bi = reference_order_shape(shape).bi();
-  int64_t tiles = 0;
-  for (const SystemDesc& d : s->sys_h) tiles += (d.n + bi - 1) / bi;
-  return static_cast<int32_t>(std::min<int64_t>(tiles, INT32_MAX));
-}
-
-// Default reference-order shape: the largest i-tiles that still give every SM at
-// least one tile (a particle's sum is never split, so a small system needs small
-// tiles to occupy the GPU); the smallest shape when none does.  Measured against the
-// fastest shape: N = 2,048 .. 65,536 take 64 x 1, N = 262,144 and 1M take 128 x 4.
-static int default_reference_order_shape(const nb_sim* s) {
-  const int last = reference_order_num_shapes() - 1;
-  for (int k = 0; k < last; ++k)
-    if (reference_order_tile_count(s, k) >= s->sms) return k;
-  return last;
-}
-
-// Tile table of the reference-order kernel for shape s->ro_shape (rebuilt when the
-// shape changes; the systems never change after creation).
-static int build_reference_order_tiles(nb_sim* s) {
-  const int bi = reference_order_shape(s->ro_shape).bi();
-  dev_free(s->ro_tiles_d);
-  std::vector<int32_t> t;
-  s->ro_first.assign(1, 0);
-  for (int32_t k = 0; k < static_cast<int32_t>(s->sys_h.size()); ++k) {
-    const int32_t count = (s->sys_h[k].n + bi - 1) / bi;
-    for (int32_t it = 0; it < count; ++it) {
-      t.push_back(k);
-      t.push_back(it);
-    }
-    s->ro_first.push_back(s->ro_first.back() + count);
-  }
-  NB_TRY(dev_alloc(&s->ro_tiles_d, t.size()));
-  NB_CUDA(cudaMemcpyAsync(s->ro_tiles_d, t.data(), t.size() * sizeof(int32_t),
-                          cudaMemcpyHostToDevice, s->stream));
-  NB_CUDA(cudaStreamSynchronize(s->stream));  // the host vector dies on return
-  int blocks = 0;
-  if (reference_order_blocks_per_sm(s->ro_shape, &blocks) != cudaSuccess || blocks < 1)
-    blocks = 1;
-  s->ro_grid = blocks * s->sms;
-  return NB_OK;
-}
-
-// Reference-order pass over systems [k0, k1): one launch over their tiles.
-static int launch_reference_order_range(nb_sim* s, const ForceArgs& a, int32_t k0, int32_t k1) {
-  const int32_t first = s->ro_first[k0];
-  const int32_t count = s->ro_first[k1] - first;
-  NB_CUDA(launch_reference_order(s->ro_shape, a,
-                                 s->ro_tiles_d + 2 * static_cast<int64_t>(first), count,
-                                 std::min(s->ro_grid, count), s->stream));
+// The duplicated j-layout buffer of the reference-order kernel.
+static int ensure_reference_order_dup(nb_sim* s) {
+  if (!s->ro_dup_d) NB_TRY(dev_alloc(&s->ro_dup_d, 2 * static_cast<size_t>(s->n_pad)));
   return NB_OK;
 }
 
@@ -345,6 +348,11 @@ int launch_with(nb_sim* s, ForceArgs a, const WorkListDev& w) {
   a.segs = w.segs;
   a.seg_begin = w.seg_begin;
   a.fix = w.fix;
+  if (w.cfg < 0) {
+    // Reference order: the duplicated layout of a.pos must have been written.
+    NB_CUDA(launch_reference_order(-1 - w.cfg, a, s->ro_dup_d, w.grid, s->stream));
+    return NB_OK;
+  }
   NB_CUDA(launch_force(w.cfg, s->params.accumulator == NB_ACC_COMPENSATED, s->per_pair_mass, a,
                        w.grid, s->stream));
   return NB_OK;
@@ -360,11 +368,13 @@ int force_pass(nb_sim* s, float4* accel_out, int per_system) {
       NB_CUDA(launch_predicated(a, s->sys_h[k], k, s->stream));
   } else if (s->params.accumulator == NB_ACC_REFERENCE_ORDER) {
     if (s->per_pair_mass) return set_error(NB_ERR_INVALID_ARGUMENT, kReferenceOrderMassError);
-    const int32_t nsys = static_cast<int32_t>(s->sys_h.size());
+    NB_TRY(ensure_reference_order_dup(s));
+    NB_CUDA(launch_reference_order_dup(a.pos, s->n_pad, s->ro_dup_d, s->stream));
     if (per_system) {
-      for (int32_t k = 0; k < nsys; ++k) NB_TRY(launch_reference_order_range(s, a, k, k + 1));
+      NB_TRY(build_per_system_worklists(s, per_system));
+      for (const auto& w : s->wl_sys) NB_TRY(launch_with(s, a, w));
     } else {
-      NB_TRY(launch_reference_order_range(s, a, 0, nsys));
+      NB_TRY(launch_with(s, a, s->ro_wl));
     }
   } else if (per_system) {
     NB_TRY(build_per_system_worklists(s, per_system));
@@ -419,6 +429,36 @@ static int default_config(nb_sim* s) {
   return default_config_for(s, 0, static_cast<int32_t>(s->sys_h.size()));
 }
 
+// i-tiles of reference-order shape `shape` over systems [first, first + count).
+static int64_t reference_order_tiles(const nb_sim* s, int shape, int32_t first, int32_t count) {
+  const int bi = reference_order_shape(shape).bi();
+  int64_t tiles = 0;
+  for (int32_t q = first; q < first + count; ++q) tiles += (s->sys_h[q].n + bi - 1) / bi;
+  return tiles;
+}
+
+// Grid of the reference-order kernel: the same number of CTAs on every SM, at
+// most the occupancy limit and at most one CTA per i-tile on average, so that each
+// CTA's share is at least one whole i-tile and a hand-over chain is never longer
+// than two parts (a particle's sum is sequential: a longer chain would run its
+// parts one after another).  Fewer i-tiles than SMs: one CTA per i-tile.
+static int reference_order_grid(nb_sim* s, int shape, int32_t first, int32_t count) {
+  const int64_t tiles = reference_order_tiles(s, shape, first, count);
+  const int occ = max_grid_for(s, -1 - shape) / s->sms;
+  const int64_t per_sm = std::min<int64_t>(occ, tiles / s->sms);
+  return static_cast<int>(per_sm >= 1 ? per_sm * s->sms : std::max<int64_t>(1, tiles));
+}
+
+// Default reference-order shape: the largest i-tiles that still give every SM at
+// least two CTAs (eight warps) by reference_order_grid; the smallest shape (the
+// most particles summed at once) when none does.
+static int default_reference_order_for(nb_sim* s, int32_t first, int32_t count) {
+  const int last = reference_order_num_shapes() - 1;
+  for (int k = 0; k < last; ++k)
+    if (reference_order_tiles(s, k, first, count) >= 2 * static_cast<int64_t>(s->sms)) return k;
+  return last;
+}
+
 static int create_impl(const nb_params* p, uint32_t num_systems, const uint32_t* sizes,
                        const float* x, const float* y, const float* z, const float* vx,
                        const float* vy, const float* vz, const float* mass, nb_sim** out) {
@@ -456,6 +496,8 @@ static int create_impl(const nb_params* p, uint32_t num_systems, const uint32_t*
     d.offset = off;
     d.n = static_cast<int32_t>(sizes[k]);
     d.npad = static_cast<int32_t>((sizes[k] + kPadQuantum - 1) / kPadQuantum * kPadQuantum);
+    d.shard_first = 0;
+    d.shard_count = 0;  // the whole system
     s->sys_h.push_back(d);
     s->user_offset.push_back(uoff);
     off += d.npad;
@@ -516,8 +558,11 @@ static int create_impl(const nb_params* p, uint32_t num_systems, const uint32_t*
     return fail(cuda_error(e, "copy state"));
   s->cfg = default_config(s);
   if ((st = build_main_worklist(s, s->cfg)) != NB_OK) return fail(st);
-  s->ro_shape = default_reference_order_shape(s);
-  if ((st = build_reference_order_tiles(s)) != NB_OK) return fail(st);
+  if (reference_order_mode(s)) {
+    s->ro_shape = default_reference_order_for(s, 0, static_cast<int32_t>(s->sys_h.size()));
+    if ((st = build_reference_order_worklist(s, s->ro_shape)) != NB_OK) return fail(st);
+    if ((st = ensure_reference_order_dup(s)) != NB_OK) return fail(st);
+  }
   if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return fail(cuda_error(e, "create"));
   *out = s;
   return NB_OK;
@@ -683,7 +728,8 @@ int nb_sim_destroy(nb_sim* s) {
   dev_free(s->err_d);
   dev_free(s->partials_d);
   dev_free(s->counters_d);
-  dev_free(s->ro_tiles_d);
+  free_worklist(s->ro_wl);
+  dev_free(s->ro_dup_d);
   release_aux(s);
   release_render_buffers(s);
   if (s->ev0) cudaEventDestroy(s->ev0);
@@ -882,11 +928,10 @@ int nb_sim_set_kernel_config(nb_sim* s, int32_t index) {
 
 int nb_sim_kernel_info(const nb_sim* s, nb_kernel_info* info) {
   if (!s || !info) return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
-  if (s->params.accumulator == NB_ACC_REFERENCE_ORDER) {
+  if (reference_order_mode(s)) {
     const KernelShape sh = reference_order_shape(s->ro_shape);
-    const int32_t tiles = s->ro_first.empty() ? 0 : s->ro_first.back();
     *info = nb_kernel_info{-1 - s->ro_shape, sh.threads, sh.r, sh.bj, sh.stages,
-                           std::min(s->ro_grid, tiles), tiles, 0};
+                           s->ro_wl.grid, s->ro_wl.nseg, s->ro_wl.split};
     return NB_OK;
   }
   const KernelShape sh = force_config_shape(s->cfg);
@@ -911,7 +956,7 @@ int nb_sim_autotune(nb_sim* s, int32_t* chosen) {
     float best_ms = 1e30f;
     for (int k = 0; k < reference_order_num_shapes(); ++k) {
       s->ro_shape = k;
-      NB_TRY(build_reference_order_tiles(s));
+      NB_TRY(build_reference_order_worklist(s, k));
       NB_TRY(force_pass(s, s->acc_d, kPerSystemNone));  // warm-up
       NB_CUDA(cudaEventRecord(s->ev0, s->stream));
       NB_TRY(force_pass(s, s->acc_d, kPerSystemNone));
@@ -925,7 +970,7 @@ int nb_sim_autotune(nb_sim* s, int32_t* chosen) {
       }
     }
     s->ro_shape = best;
-    NB_TRY(build_reference_order_tiles(s));
+    NB_TRY(build_reference_order_worklist(s, best));
     if (chosen) *chosen = -1 - best;
     return NB_OK;
   }
@@ -997,6 +1042,96 @@ int nb_plan_work(uint32_t num_systems, const uint32_t* sizes, int32_t config_ind
   return NB_OK;
 }
 
+int nb_sim_set_shard(nb_sim* s, uint64_t first, uint64_t count) {
+  if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
+  DeviceGuard dg_(s->device);
+  if (s->sys_h.size() != 1)
+    return set_error(NB_ERR_INVALID_ARGUMENT, "a shard splits a simulation of one system");
+  if (s->params.calc_method != NB_BRANCH)
+    return set_error(NB_ERR_INVALID_ARGUMENT, "shards need the BRANCH method");
+  SystemDesc& d = s->sys_h[0];
+  const uint64_t n = static_cast<uint64_t>(d.n);
+  if (count == 0) {
+    first = 0;
+    count = n;
+  }
+  if (first % kPadQuantum || first >= n || count > n - first)
+    return set_error(NB_ERR_INVALID_ARGUMENT,
+                     "a shard is [first, first + count) within the system, first a multiple of 16");
+  if (first + count != n && count % kPadQuantum)
+    return set_error(NB_ERR_INVALID_ARGUMENT,
+                     "a shard's count is a multiple of 16 unless the shard ends the system");
+  d.shard_first = static_cast<int32_t>(first);
+  d.shard_count = (first == 0 && count == n) ? 0 : static_cast<int32_t>(count);
+  NB_TRY(upload_systems(s));
+  NB_TRY(build_main_worklist(s, s->cfg));
+  if (reference_order_mode(s)) NB_TRY(build_reference_order_worklist(s, s->ro_shape));
+  for (auto& w : s->wl_sys) free_worklist(w);
+  s->wl_sys.clear();
+  s->wl_sys_policy = -1;
+  s->adj.valid = false;
+  NB_CUDA(cudaStreamSynchronize(s->stream));
+  return NB_OK;
+}
+
+// Byte range of particles [first, first + count) of a one-system simulation's
+// state arrays (16 bytes per particle in both the position and the velocity
+// buffer); a block that ends the system runs to its padded end.
+static int state_block(const nb_sim* s, uint64_t first, uint64_t count, int32_t what,
+                       size_t* offset, size_t* bytes) {
+  if (s->sys_h.size() != 1)
+    return set_error(NB_ERR_INVALID_ARGUMENT, "state blocks address a simulation of one system");
+  if (what != NB_BLOCK_POSITIONS && what != NB_BLOCK_VELOCITIES)
+    return set_error(NB_ERR_INVALID_ARGUMENT, "what must be NB_BLOCK_POSITIONS or _VELOCITIES");
+  const SystemDesc& d = s->sys_h[0];
+  const uint64_t n = static_cast<uint64_t>(d.n);
+  if (count == 0 || first % kPadQuantum || first >= n || count > n - first)
+    return set_error(NB_ERR_INVALID_ARGUMENT,
+                     "a block is [first, first + count) within the system, first a multiple of 16");
+  const uint64_t end = (first + count == n) ? static_cast<uint64_t>(d.npad) : first + count;
+  if (end % kPadQuantum)
+    return set_error(NB_ERR_INVALID_ARGUMENT,
+                     "a block's count is a multiple of 16 unless the block ends the system");
+  *offset = 16 * first;
+  *bytes = 16 * (end - first);
+  return NB_OK;
+}
+
+int nb_sim_state_block_bytes(const nb_sim* s, uint64_t first, uint64_t count, int32_t what,
+                             uint64_t* bytes) {
+  if (!s || !bytes) return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
+  size_t off = 0, b = 0;
+  NB_TRY(state_block(s, first, count, what, &off, &b));
+  *bytes = b;
+  return NB_OK;
+}
+
+int nb_sim_copy_state_block(nb_sim* s, uint64_t first, uint64_t count, int32_t what,
+                            void* dst_device) {
+  if (!s || !dst_device) return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard dg_(s->device);
+  size_t off = 0, bytes = 0;
+  NB_TRY(state_block(s, first, count, what, &off, &bytes));
+  const unsigned char* src = what == NB_BLOCK_POSITIONS
+                                 ? reinterpret_cast<const unsigned char*>(s->pos_d[s->cur])
+                                 : reinterpret_cast<const unsigned char*>(s->vel_d);
+  NB_CUDA(cudaMemcpyAsync(dst_device, src + off, bytes, cudaMemcpyDeviceToDevice, s->stream));
+  return NB_OK;
+}
+
+int nb_sim_load_state_block(nb_sim* s, uint64_t first, uint64_t count, int32_t what,
+                            const void* src_device) {
+  if (!s || !src_device) return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard dg_(s->device);
+  size_t off = 0, bytes = 0;
+  NB_TRY(state_block(s, first, count, what, &off, &bytes));
+  unsigned char* dst = what == NB_BLOCK_POSITIONS
+                           ? reinterpret_cast<unsigned char*>(s->pos_d[s->cur])
+                           : reinterpret_cast<unsigned char*>(s->vel_d);
+  NB_CUDA(cudaMemcpyAsync(dst + off, src_device, bytes, cudaMemcpyDeviceToDevice, s->stream));
+  return NB_OK;
+}
+
 int nb_sim_generate(nb_sim* s, int32_t kind, uint64_t seed) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
   DeviceGuard dg_(s->device);
@@ -1059,13 +1194,7 @@ int nb_sim_graph_capture(nb_sim* s, int32_t iterations) {
   if (s->params.calc_method == NB_PREDICATED &&
       static_cast<int64_t>(s->sys_h.size()) * iterations > 65536)
     return set_error(NB_ERR_INVALID_ARGUMENT, "too many launches to capture");
-  for (int b = 0; b < 2; ++b) {
-    if (s->gexec[b]) cudaGraphExecDestroy(s->gexec[b]);
-    if (s->graph[b]) cudaGraphDestroy(s->graph[b]);
-    s->gexec[b] = nullptr;
-    s->graph[b] = nullptr;
-  }
-  s->graph_iters = 0;
+  drop_graphs(s);
   // The launches bake in the buffer pointers, so keep one graph per starting buffer.
   const int cur0 = s->cur;
   for (int b = 0; b < 2; ++b) {

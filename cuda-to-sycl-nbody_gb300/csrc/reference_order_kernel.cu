@@ -9,14 +9,30 @@
 // particle, so on the same GPU its results are bit-identical to the reference
 // kernel's.  The fast kernel (force_kernel.cuh) sums in another order instead.
 //
-// GB300 layout: the two lanes of each packed FP32x2 register pair hold two
-// different i-particles (each lane its own running sum, so the order per particle
-// is untouched), and j-tiles are staged in shared memory already duplicated as
-// (x, x, y, y) (z, z, m, m), so one broadcast 16-byte load feeds both lanes.  A
-// CTA owns whole i-tiles: an i-particle's sum is never split.  Only the n real
-// particles of a system are summed (no padding terms), as in the reference.
-// Each CTA prefetches the next j-tile into registers while it computes the
-// current one (double-buffered shared memory, no device-side waits).
+// GB300 design:
+//   * The two lanes of each packed FP32x2 register pair hold two different
+//     i-particles (each lane its own running sum, so the order per particle is
+//     untouched).  j-particles come from a copy of the positions laid out
+//     duplicated, (x, x, y, y) (z, z, m, m) per particle (ro_dup_kernel, one pass
+//     per step), so one broadcast 16-byte shared load feeds both lanes.
+//   * j-tiles of that copy are staged global -> shared by cp.async.bulk into a
+//     STAGES-deep ring with mbarrier completion, like the fast kernel.
+//   * Persistent grid with a stream-K work list (worklist.hpp): every CTA gets
+//     the same number of pair interactions to within one j-tile, whatever the
+//     number of i-tiles, so the last wave is never part-empty.  A particle's sum
+//     cannot be split into independently summed parts, so an i-tile whose j-range
+//     is cut between CTAs is *handed over* instead: the part over the first
+//     j-tiles stores its running sums, and the CTA owning the next part starts
+//     from them, in j order -- the same sequence of roundings as one CTA.  Each
+//     CTA walks its segments last to first: the part it hands over (its last
+//     segment) is done first and the part it continues (its first segment) last,
+//     so by the time a CTA needs its predecessor's sums they are long written.
+//     The launch is cooperative (all CTAs resident), and every wait -- on an
+//     mbarrier or on a predecessor -- is bounded (2 s of %globaltimer); on
+//     timeout the CTA sets bit 0 of the error word, drains its own copies and
+//     exits.
+//   * Only the n real particles of a system are summed (no padding terms), as in
+//     the reference.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -28,28 +44,102 @@
 namespace nbg {
 namespace {
 
-// Shapes: kRoThreads threads per CTA, kRoPairs i-pairs per thread, so i-tiles of
-// kRoThreads * 2 * kRoPairs particles.  A particle's sum cannot be split, so small
-// systems need small i-tiles to give every SM work (see the shape table below).
-constexpr int kRoBJ = 256;       // j-particles per shared-memory tile
-constexpr int kRoRecs = kRoBJ / 2;                // 32-byte pair records per j-tile
-constexpr int kRoUnroll = 4;     // j steps per unrolled block
+constexpr int kRoBJ = 256;     // j-particles per shared-memory tile
+constexpr int kRoStages = 3;   // depth of the tile ring
+constexpr int kRoUnroll = 4;   // j steps per unrolled block
+constexpr uint64_t kRoWaitNs = 2000000000ull;
+
+__device__ __forceinline__ uint32_t ro_smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t ro_global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void ro_mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(ro_smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void ro_fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void ro_fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void ro_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ro_smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Bulk copy global -> shared; both addresses 16-byte aligned, bytes % 16 == 0.
+__device__ __forceinline__ void ro_bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          ro_smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(ro_smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool ro_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(ro_smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait on phase `parity`; false after kRoWaitNs.
+__device__ __noinline__ bool ro_wait_slow(uint64_t* bar, uint32_t parity) {
+  const uint64_t t0 = ro_global_ns();
+  while (true) {
+    if (ro_try_wait(bar, parity)) return true;
+    if (ro_global_ns() - t0 > kRoWaitNs) return false;
+  }
+}
+
+__device__ __forceinline__ bool ro_wait(uint64_t* bar, uint32_t parity) {
+  if (ro_try_wait(bar, parity)) return true;
+  return ro_wait_slow(bar, parity);
+}
+
+// Bounded wait until the hand-over counter reaches `target`; false after kRoWaitNs.
+__device__ __noinline__ bool ro_wait_counter(const int32_t* counter, int32_t target) {
+  const volatile int32_t* c = counter;
+  const uint64_t t0 = ro_global_ns();
+  while (*c < target) {
+    if (ro_global_ns() - t0 > kRoWaitNs) return false;
+    __nanosleep(64);
+  }
+  __threadfence();
+  return true;
+}
 
 // One j step against all of the thread's i-pairs.  kDiag: the tile overlaps the
 // i-tile, so the term of j == i is left out of that lane's sum (the reference's
 // `if (i == id) continue;`), by keeping the old value rather than adding zero.
-template <int kRoPairs, bool kDiag>
+template <int P, bool kDiag>
 __device__ __forceinline__ void ro_step(const float4 xy, const float4 zm, float2 e2,
-                                        const float2 (&nx)[kRoPairs],
-                                        const float2 (&ny)[kRoPairs],
-                                        const float2 (&nz)[kRoPairs], float2 (&ax)[kRoPairs],
-                                        float2 (&ay)[kRoPairs], float2 (&az)[kRoPairs], int j,
-                                        const int (&li)[kRoPairs]) {
+                                        const float2 (&nx)[P], const float2 (&ny)[P],
+                                        const float2 (&nz)[P], float2 (&ax)[P],
+                                        float2 (&ay)[P], float2 (&az)[P], int j,
+                                        const int (&li)[P]) {
   const float2 xx = make_float2(xy.x, xy.y);
   const float2 yy = make_float2(xy.z, xy.w);
   const float2 zz = make_float2(zm.x, zm.y);
 #pragma unroll
-  for (int k = 0; k < kRoPairs; ++k) {
+  for (int k = 0; k < P; ++k) {
     // r = other_pos - pos (:200)
     const float2 rx = __fadd2_rn(xx, nx[k]);
     const float2 ry = __fadd2_rn(yy, ny[k]);
@@ -89,56 +179,120 @@ __device__ __forceinline__ void ro_step(const float4 xy, const float4 zm, float2
 }
 
 // Steps over j = j0 .. j0 + count - 1 of the staged tile, in order.
-template <int kRoPairs, bool kDiag>
+template <int P, bool kDiag>
 __device__ __forceinline__ void ro_tile(const float4* __restrict__ tile, int count, int j0,
-                                        float2 e2, const float2 (&nx)[kRoPairs],
-                                        const float2 (&ny)[kRoPairs],
-                                        const float2 (&nz)[kRoPairs], float2 (&ax)[kRoPairs],
-                                        float2 (&ay)[kRoPairs], float2 (&az)[kRoPairs],
-                                        const int (&li)[kRoPairs]) {
+                                        float2 e2, const float2 (&nx)[P], const float2 (&ny)[P],
+                                        const float2 (&nz)[P], float2 (&ax)[P], float2 (&ay)[P],
+                                        float2 (&az)[P], const int (&li)[P]) {
   int jj = 0;
 #pragma unroll 1
   for (; jj + kRoUnroll <= count; jj += kRoUnroll) {
 #pragma unroll
     for (int u = 0; u < kRoUnroll; ++u)
-      ro_step<kRoPairs, kDiag>(tile[2 * (jj + u)], tile[2 * (jj + u) + 1], e2, nx, ny, nz, ax, ay, az,
-                     j0 + jj + u, li);
+      ro_step<P, kDiag>(tile[2 * (jj + u)], tile[2 * (jj + u) + 1], e2, nx, ny, nz, ax, ay, az,
+                        j0 + jj + u, li);
   }
 #pragma unroll 1
   for (; jj < count; ++jj)
-    ro_step<kRoPairs, kDiag>(tile[2 * jj], tile[2 * jj + 1], e2, nx, ny, nz, ax, ay, az, j0 + jj, li);
+    ro_step<P, kDiag>(tile[2 * jj], tile[2 * jj + 1], e2, nx, ny, nz, ax, ay, az, j0 + jj, li);
 }
 
-struct RoTile {
-  int32_t sys;
-  int32_t itile;
-};
+// The duplicated j-layout from the pair layout: one thread per pair record.
+__global__ void ro_dup_kernel(const float4* __restrict__ pos4, int64_t records,
+                              float4* __restrict__ dup) {
+  for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < records;
+       r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const float4 A = pos4[2 * r];      // (x0, x1, y0, y1)
+    const float4 B = pos4[2 * r + 1];  // (z0, z1, m0, m1)
+    dup[4 * r + 0] = make_float4(A.x, A.x, A.z, A.z);
+    dup[4 * r + 1] = make_float4(B.x, B.x, B.z, B.z);
+    dup[4 * r + 2] = make_float4(A.y, A.y, A.w, A.w);
+    dup[4 * r + 3] = make_float4(B.y, B.y, B.w, B.w);
+  }
+}
 
-template <int kRoThreads, int kRoPairs>
-__global__ void __launch_bounds__(kRoThreads) reference_order_kernel(const ForceArgs a,
-                                                                      const RoTile* tiles,
-                                                                      int32_t num_tiles) {
-  constexpr int kRoBI = kRoThreads * 2 * kRoPairs;  // i-particles per tile
-  constexpr int kRoRecsPerThread = (kRoRecs + kRoThreads - 1) / kRoThreads;
-  static_assert(kRoBI % kPadQuantum == 0, "i-tiles must hold whole padding quanta");
-  // [buffer][j][2]: (x, x, y, y), (z, z, m, m)
-  __shared__ __align__(16) float4 sm[2][kRoBJ * 2];
+template <int THREADS, int P>
+__global__ void __launch_bounds__(THREADS) reference_order_kernel(const ForceArgs a,
+                                                                  const float4* __restrict__ dup) {
+  constexpr int BI = THREADS * 2 * P;  // i-particles per i-tile
+  static_assert(BI % kPadQuantum == 0, "i-tiles must hold whole padding quanta");
+  __shared__ __align__(128) float4 ring[kRoStages][kRoBJ * 2];
+  __shared__ __align__(8) uint64_t full_bar[kRoStages];
+  __shared__ int s_bail;
+
   const int tid = threadIdx.x;
+  const int seg_lo = a.seg_begin[blockIdx.x];
+  const int seg_hi = a.seg_begin[blockIdx.x + 1];
+  if (seg_lo >= seg_hi) return;
+
+  if (tid == 0) {
+#pragma unroll
+    for (int s = 0; s < kRoStages; ++s) ro_mbar_init(&full_bar[s], 1);
+    ro_fence_mbar_init();
+    s_bail = 0;
+  }
+  __syncthreads();
+
+  // Producer cursor (thread 0): segments last to first, j-tiles in order within each.
+  int p_seg = seg_hi - 1;
+  int p_jt = a.segs[p_seg].jt0;
+  uint32_t issued = 0;
+  auto produce = [&]() {
+    if (p_seg < seg_lo) return;
+    const Segment& sg = a.segs[p_seg];
+    const SystemDesc& sd = a.sys[sg.sys];
+    const int count = min(kRoBJ, sd.n - p_jt * kRoBJ);
+    const int64_t first = sd.offset + static_cast<int64_t>(p_jt) * kRoBJ;
+    const uint32_t slot = issued % kRoStages;
+    // Failure-detection test: leave the first tile's barrier without arrival or
+    // copy, so the consumers' bounded wait on it runs out.
+    if (!(a.skip_first_tile && issued == 0)) {
+      ro_fence_proxy_async();
+      ro_arrive_expect_tx(&full_bar[slot], static_cast<uint32_t>(count) * 32u);
+      ro_bulk_g2s(&ring[slot][0], dup + 2 * first, static_cast<uint32_t>(count) * 32u,
+                  &full_bar[slot]);
+    }
+    ++issued;
+    if (++p_jt >= sg.jt1) {
+      --p_seg;
+      if (p_seg >= seg_lo) p_jt = a.segs[p_seg].jt0;
+    }
+  };
+  if (tid == 0) {
+#pragma unroll
+    for (int k = 0; k < kRoStages - 1; ++k) produce();
+  }
+
   const float4* pos4 = reinterpret_cast<const float4*>(a.pos);
   const float2 e2 = make_float2(a.eps2, a.eps2);
+  uint32_t consumed = 0;
 
-  for (int32_t t = blockIdx.x; t < num_tiles; t += gridDim.x) {
-    const RoTile tl = tiles[t];
-    const SystemDesc sd = a.sys[tl.sys];
-    const int ibase = tl.itile * kRoBI;
+  // Give up: flag the error, drain this CTA's copies still in flight (bounded) and
+  // leave without touching the outputs.
+  auto bail = [&]() {
+    if (tid == 0) {
+      atomicOr(a.err, 1);
+      for (uint32_t k = consumed; k < issued; ++k)
+        (void)ro_wait(&full_bar[k % kRoStages], (k / kRoStages) & 1u);
+    }
+  };
+
+  for (int sgi = seg_hi - 1; sgi >= seg_lo; --sgi) {
+    const Segment sg = a.segs[sgi];
+    const SystemDesc sd = a.sys[sg.sys];
+    const int ibase = sd.shard_first + sg.itile * BI;
+    const int iend = shard_end(sd);
     const int64_t rec0 = sd.offset >> 1;  // first pair record of the system
     const int last_rec = (sd.npad >> 1) - 1;
+    const bool split = sg.fix >= 0;
+    const Fixup fx = split ? a.fix[sg.fix] : Fixup{1, 0};
+    float4* slots = a.partials + static_cast<int64_t>(fx.slot0) * BI;
 
-    float2 nx[kRoPairs], ny[kRoPairs], nz[kRoPairs], ax[kRoPairs], ay[kRoPairs], az[kRoPairs];
-    int li[kRoPairs];
+    float2 nx[P], ny[P], nz[P], ax[P], ay[P], az[P];
+    int li[P];
 #pragma unroll
-    for (int k = 0; k < kRoPairs; ++k) {
-      li[k] = ibase + 2 * (k * kRoThreads + tid);
+    for (int k = 0; k < P; ++k) {
+      li[k] = ibase + 2 * (k * THREADS + tid);
       const int r = min(li[k] >> 1, last_rec);  // lanes past the system read its last record
       const float4 A = pos4[(rec0 + r) * 2];      // (x0, x1, y0, y1)
       const float4 B = pos4[(rec0 + r) * 2 + 1];  // (z0, z1, m0, m1)
@@ -148,60 +302,68 @@ __global__ void __launch_bounds__(kRoThreads) reference_order_kernel(const Force
       ax[k] = ay[k] = az[k] = make_float2(0.f, 0.f);
     }
 
-    const int ntiles_j = (sd.n + kRoBJ - 1) / kRoBJ;
-    float4 pa[kRoRecsPerThread], pb[kRoRecsPerThread];
-    // Stage j-tile jt's records (only those holding real particles) into registers.
-    auto fetch = [&](int jt) {
-      const int nrec = (min(kRoBJ, sd.n - jt * kRoBJ) + 1) >> 1;
-#pragma unroll
-      for (int q = 0; q < kRoRecsPerThread; ++q) {
-        const int r = q * kRoThreads + tid;
-        if (r < nrec) {
-          const int64_t g = rec0 + jt * kRoRecs + r;
-          pa[q] = pos4[g * 2];
-          pb[q] = pos4[g * 2 + 1];
-        }
-      }
-    };
-    auto stage = [&](int jt, int buf) {
-      const int nrec = (min(kRoBJ, sd.n - jt * kRoBJ) + 1) >> 1;
-#pragma unroll
-      for (int q = 0; q < kRoRecsPerThread; ++q) {
-        const int r = q * kRoThreads + tid;
-        if (r < nrec) {
-          float4* d = &sm[buf][4 * r];
-          d[0] = make_float4(pa[q].x, pa[q].x, pa[q].z, pa[q].z);
-          d[1] = make_float4(pb[q].x, pb[q].x, pb[q].z, pb[q].z);
-          d[2] = make_float4(pa[q].y, pa[q].y, pa[q].w, pa[q].w);
-          d[3] = make_float4(pb[q].y, pb[q].y, pb[q].w, pb[q].w);
-        }
-      }
-    };
-
-    __syncthreads();  // the previous i-tile's last reads of sm[] are done
-    fetch(0);
-    stage(0, 0);
-    __syncthreads();
-    for (int jt = 0; jt < ntiles_j; ++jt) {
-      const int buf = jt & 1;
-      if (jt + 1 < ntiles_j) fetch(jt + 1);
-      const int j0 = jt * kRoBJ;
-      const int count = min(kRoBJ, sd.n - j0);
-      const bool diag = (j0 < ibase + kRoBI) && (ibase < j0 + count);
-      if (diag)
-        ro_tile<kRoPairs, true>(sm[buf], count, j0, e2, nx, ny, nz, ax, ay, az, li);
-      else
-        ro_tile<kRoPairs, false>(sm[buf], count, j0, e2, nx, ny, nz, ax, ay, az, li);
-      if (jt + 1 < ntiles_j) stage(jt + 1, buf ^ 1);
+    if (split && sg.part > 0) {
+      // Continue the running sums where the previous part of this i-tile stopped.
+      if (tid == 0 && !ro_wait_counter(&a.counters[sg.fix], sg.part)) s_bail = 1;
       __syncthreads();
+      if (s_bail) {
+        bail();
+        return;
+      }
+      const float4* in = slots + static_cast<int64_t>(sg.part - 1) * BI;
+#pragma unroll
+      for (int k = 0; k < P; ++k) {
+        const int idx = k * THREADS + tid;
+        const float4 u = __ldcg(&in[2 * idx]);
+        const float4 w = __ldcg(&in[2 * idx + 1]);
+        ax[k] = make_float2(u.x, u.y);
+        ay[k] = make_float2(u.z, u.w);
+        az[k] = make_float2(w.x, w.y);
+      }
     }
 
+    bool timed_out = false;
+    for (int jt = sg.jt0; jt < sg.jt1; ++jt, ++consumed) {
+      if (tid == 0) produce();
+      const uint32_t slot = consumed % kRoStages;
+      if (!ro_wait(&full_bar[slot], (consumed / kRoStages) & 1u)) timed_out = true;
+      const int j0 = jt * kRoBJ;
+      const int count = min(kRoBJ, sd.n - j0);
+      const bool diag = (j0 < ibase + BI) && (ibase < j0 + count);
+      if (!timed_out) {
+        if (diag)
+          ro_tile<P, true>(ring[slot], count, j0, e2, nx, ny, nz, ax, ay, az, li);
+        else
+          ro_tile<P, false>(ring[slot], count, j0, e2, nx, ny, nz, ax, ay, az, li);
+      }
+      if (__syncthreads_or(timed_out)) {
+        bail();
+        return;
+      }
+    }
+
+    if (split && sg.part < fx.nparts - 1) {
+      // Hand the running sums to the CTA that owns the next part.
+      float4* out = slots + static_cast<int64_t>(sg.part) * BI;
 #pragma unroll
-    for (int k = 0; k < kRoPairs; ++k) {
-      if (li[k] < sd.n)
+      for (int k = 0; k < P; ++k) {
+        const int idx = k * THREADS + tid;
+        __stcg(&out[2 * idx], make_float4(ax[k].x, ax[k].y, ay[k].x, ay[k].y));
+        __stcg(&out[2 * idx + 1], make_float4(az[k].x, az[k].y, 0.f, 0.f));
+      }
+      __threadfence();
+      __syncthreads();
+      if (tid == 0) atomicAdd(&a.counters[sg.fix], 1);
+      continue;
+    }
+    if (split && tid == 0) a.counters[sg.fix] = 0;  // every part has run: reset for the next launch
+
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+      if (li[k] < iend)
         finish_particle(a, sd, sd.offset + li[k], ax[k].x, ay[k].x, az[k].x, -nx[k].x, -ny[k].x,
                         -nz[k].x);
-      if (li[k] + 1 < sd.n)
+      if (li[k] + 1 < iend)
         finish_particle(a, sd, sd.offset + li[k] + 1, ax[k].y, ay[k].y, az[k].y, -nx[k].y,
                         -ny[k].y, -nz[k].y);
     }
@@ -211,11 +373,10 @@ __global__ void __launch_bounds__(kRoThreads) reference_order_kernel(const Force
 struct RoShapeEntry {
   int threads;
   int pairs;
-  void (*kernel)(const ForceArgs, const RoTile*, int32_t);
+  void (*kernel)(const ForceArgs, const float4*);
 };
 
-// Largest i-tiles first.  Measured at N = 1M: 128 x 4 64.4 %, 128 x 2 62.8 % of FP32
-// peak; the 64 x 1 shape gives a 25,600-particle system 200 CTAs instead of 25.
+// Largest i-tiles first.
 const RoShapeEntry kRoShapes[] = {
     {128, 4, reference_order_kernel<128, 4>},
     {128, 2, reference_order_kernel<128, 2>},
@@ -229,7 +390,7 @@ int reference_order_num_shapes() { return kNumRoShapes; }
 
 KernelShape reference_order_shape(int index) {
   const RoShapeEntry& e = kRoShapes[index];
-  return KernelShape{e.threads, 2 * e.pairs, kRoBJ, 2};
+  return KernelShape{e.threads, 2 * e.pairs, kRoBJ, kRoStages};
 }
 
 cudaError_t reference_order_blocks_per_sm(int index, int* blocks) {
@@ -237,12 +398,32 @@ cudaError_t reference_order_blocks_per_sm(int index, int* blocks) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, e.kernel, e.threads, 0);
 }
 
-cudaError_t launch_reference_order(int index, const ForceArgs& a, const int32_t* tiles,
-                                   int32_t num_tiles, int grid, cudaStream_t stream) {
-  if (num_tiles <= 0) return cudaSuccess;
-  const RoShapeEntry& e = kRoShapes[index];
-  e.kernel<<<grid, e.threads, 0, stream>>>(a, reinterpret_cast<const RoTile*>(tiles), num_tiles);
+cudaError_t launch_reference_order_dup(const float* pos, int64_t n_pad_total, float4* dup,
+                                       cudaStream_t stream) {
+  const int64_t records = n_pad_total / 2;
+  const int threads = 256;
+  const int64_t blocks = (records + threads - 1) / threads;
+  ro_dup_kernel<<<static_cast<int>(blocks < 65535 * 16 ? blocks : 65535 * 16), threads, 0,
+                  stream>>>(reinterpret_cast<const float4*>(pos), records, dup);
   return cudaGetLastError();
+}
+
+cudaError_t launch_reference_order(int index, const ForceArgs& a, const float4* dup, int grid,
+                                   cudaStream_t stream) {
+  const RoShapeEntry& e = kRoShapes[index];
+  // Cooperative: every CTA is resident, so a CTA waiting for its predecessor's
+  // hand-over always waits on a running CTA.
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(e.threads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, e.kernel, a, dup);
 }
 
 }  // namespace nbg

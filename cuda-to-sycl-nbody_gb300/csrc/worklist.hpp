@@ -1,7 +1,8 @@
 // Stream-K work-list planner for the persistent force kernel (host only).
 //
 // The unit of work is one (system, i-tile, j-tile) block of bi x |j-tile| pair
-// interactions.  Units are laid out in (system, i-tile, j-tile) order and each
+// interactions; a system's i-tiles cover its shard (SystemDesc::shard_first ..
+// shard_end), its j-tiles all of it.  Units are laid out in (system, i-tile, j-tile) order and each
 // is charged its j-tile length.  CTA k receives the units whose starting charge
 // c satisfies floor(c * grid / total) == k, i.e. one contiguous run of the
 // sequence with total / grid charge (+- one tile).  A run that covers only part
@@ -48,7 +49,7 @@ bool plan_work_into(const SystemDesc* sys, int32_t first, int32_t count, int32_t
                     int32_t max_grid, Out& out, int32_t* slots_out, int32_t* split_out) {
   int64_t total = 0, tiles = 0;
   for (int32_t s = first; s < first + count; ++s) {
-    const int64_t nit = (sys[s].n + bi - 1) / bi;
+    const int64_t nit = (shard_end(sys[s]) - sys[s].shard_first + bi - 1) / bi;
     const int64_t njt = (sys[s].npad + bj - 1) / bj;
     total += nit * sys[s].npad;
     tiles += nit * njt;
@@ -63,7 +64,7 @@ bool plan_work_into(const SystemDesc* sys, int32_t first, int32_t count, int32_t
   int64_t next_cta = 0;    // first CTA whose seg_begin is not yet set
   int32_t slots = 0, split = 0;
   for (int32_t s = first; s < first + count; ++s) {
-    const int32_t nit = (sys[s].n + bi - 1) / bi;
+    const int32_t nit = (shard_end(sys[s]) - sys[s].shard_first + bi - 1) / bi;
     const int32_t njt = (sys[s].npad + bj - 1) / bj;
     for (int32_t it = 0; it < nit; ++it) {
       const int64_t seg_first = out.num_segments();

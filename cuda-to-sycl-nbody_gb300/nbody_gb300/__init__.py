@@ -33,6 +33,8 @@ PREDICATED = 1
 ACC_PLAIN = 0
 ACC_COMPENSATED = 1
 ACC_REFERENCE_ORDER = 2
+BLOCK_POSITIONS = 1
+BLOCK_VELOCITIES = 2
 IC_THIN_DISK = 1
 IC_PLUMMER = 2
 IC_TWO_DISKS = 3
@@ -138,6 +140,10 @@ SIGNATURES = {
     "nb_sim_adjoint_backward": (C.c_int, [_P] + [_F] * 4),
     "nb_sim_adjoint_backward_device": (C.c_int, [_P] * 5),
     "nb_accelerations_noalloc": (C.c_int, [_P, C.c_uint64, C.c_float, C.c_float, _P, _P]),
+    "nb_sim_set_shard": (C.c_int, [_P, C.c_uint64, C.c_uint64]),
+    "nb_sim_state_block_bytes": (C.c_int, [_P, C.c_uint64, C.c_uint64, C.c_int32, _U64]),
+    "nb_sim_copy_state_block": (C.c_int, [_P, C.c_uint64, C.c_uint64, C.c_int32, _P]),
+    "nb_sim_load_state_block": (C.c_int, [_P, C.c_uint64, C.c_uint64, C.c_int32, _P]),
     "nb_ic_thin_disk": (C.c_int, [C.c_uint64, C.c_uint64, C.c_float] + [_F] * 7),
     "nb_ic_plummer": (C.c_int, [C.c_uint64, C.c_uint64] + [_F] * 7),
     "nb_ic_two_disks": (C.c_int, [C.c_uint64, C.c_uint64, C.c_float] + [_F] * 7),
@@ -453,6 +459,21 @@ class Simulation:
     def export_device(self, pos_ptr: int, vel_ptr: int | None = None) -> None:
         _check(lib.nb_sim_export_device(self._h, C.c_void_p(pos_ptr),
                                         C.c_void_p(vel_ptr) if vel_ptr else None))
+
+    # shards of one system (nb_sim_set_shard); see nbody_gb300.shard
+    def set_shard(self, first: int, count: int) -> None:
+        _check(lib.nb_sim_set_shard(self._h, first, count))
+
+    def state_block_bytes(self, first: int, count: int, what: int = BLOCK_POSITIONS) -> int:
+        v = C.c_uint64()
+        _check(lib.nb_sim_state_block_bytes(self._h, first, count, what, C.byref(v)))
+        return v.value
+
+    def copy_state_block(self, first: int, count: int, what: int, dst_ptr: int) -> None:
+        _check(lib.nb_sim_copy_state_block(self._h, first, count, what, C.c_void_p(dst_ptr)))
+
+    def load_state_block(self, first: int, count: int, what: int, src_ptr: int) -> None:
+        _check(lib.nb_sim_load_state_block(self._h, first, count, what, C.c_void_p(src_ptr)))
 
     def set_stream(self, stream_ptr: int | None) -> None:
         _check(lib.nb_sim_set_stream(self._h, C.c_void_p(stream_ptr) if stream_ptr else None))

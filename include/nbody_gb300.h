@@ -227,6 +227,35 @@ int nb_sim_set_stream(nb_sim* s, void* stream);
  * Stream-ordered on the simulation's stream. */
 int nb_sim_export_device(nb_sim* s, float* pos_xyzm_device, float* vel_xyzw_device);
 
+/* ---- one system split over several GPUs or processes ---------------------------- */
+/* No reference counterpart: the reference runs its one system on device 0
+ * (simulator.cu:40, launches :59-63).  A system of n particles splits into shards,
+ * one per GPU (or process): every shard owner keeps a whole copy of the system,
+ * integrates only its own particles, each against all n, and between steps the
+ * owners exchange the position blocks of their shards (an all-gather of
+ * nb_sim_copy_state_block / nb_sim_load_state_block, for instance over NCCL).
+ * The Python ShardedSimulation (nbody_gb300.shard) does exactly that. */
+typedef enum nb_block_kind { NB_BLOCK_POSITIONS = 1, NB_BLOCK_VELOCITIES = 2 } nb_block_kind;
+/* From now on this one-system simulation's force passes integrate only particles
+ * [first, first + count): their next positions and velocities are written, the
+ * others' are not.  first is a multiple of 16, and so is count unless the shard
+ * ends the system; count = 0 restores the whole system.  Drops any captured graph;
+ * the adjoint needs the whole system.  BRANCH method only. */
+int nb_sim_set_shard(nb_sim* s, uint64_t first, uint64_t count);
+/* Size in bytes of the state block of particles [first, first + count) (16 bytes per
+ * particle; a block that ends the system is padded to a multiple of 16 particles). */
+int nb_sim_state_block_bytes(const nb_sim* s, uint64_t first, uint64_t count, int32_t what,
+                             uint64_t* bytes);
+/* Copy the current positions (what = NB_BLOCK_POSITIONS) or velocities of particles
+ * [first, first + count) to, or from, device memory, in the library's own layout:
+ * the bytes are only for another simulation of the same system (another shard's
+ * owner).  Same rules for first and count as nb_sim_set_shard.  Stream-ordered on
+ * the simulation's stream. */
+int nb_sim_copy_state_block(nb_sim* s, uint64_t first, uint64_t count, int32_t what,
+                            void* dst_device);
+int nb_sim_load_state_block(nb_sim* s, uint64_t first, uint64_t count, int32_t what,
+                            const void* src_device);
+
 /* ---- kernel selection ---------------------------------------------------------- */
 /* The compiled shapes of the tuned kernel.  No reference counterpart: the
  * reference launches ceil(N / gwSize) blocks of gwSize threads (simulator.cu:49-50),

@@ -295,6 +295,9 @@ def test_null_handles_are_rejected_without_touching_the_device():
            (L.nb_sim_adjoint_forward, (h, 1, 1)),
            (L.nb_sim_adjoint_backward, (h, None, None, None, None)),
            (L.nb_sim_adjoint_backward_device, (h, None, None, None, None)),
+           (L.nb_sim_set_shard, (h, 0, 0)), (L.nb_sim_state_block_bytes, (h, 0, 16, 1, None)),
+           (L.nb_sim_copy_state_block, (h, 0, 16, 1, None)),
+           (L.nb_sim_load_state_block, (h, 0, 16, 1, None)),
            (L.nb_sim_render, (h, None, None, 64, 64, None)),
            (L.nb_sim_time_iterations, (h, 1, 0, None))]
     for fn, args in one:
