@@ -363,6 +363,94 @@ def run_ours(args, rank, world) -> dict:
     return result
 
 
+def run_split(args, rank, world) -> dict:
+    """One 1,048,576-particle system split over the job's GPUs (strong scaling): each
+    rank integrates its shard of the particles against all N and the ranks
+    all-gather their shards' positions after every step (nbody_gb300.shard over
+    NCCL).  The timed step includes the all-gather."""
+    import torch
+    import torch.distributed as dist
+
+    import nbody_gb300 as nb
+    from nbody_gb300.shard import ShardedSimulation
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if not dist.is_initialized():                    # one GPU: a one-rank NCCL group
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        os.environ.setdefault("MASTER_PORT", "29517")
+        dist.init_process_group("nccl", rank=0, world_size=1)
+    n = args.n
+    pos, vel, m = plummer_inputs(n)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(max(1, args.flush_mib) << 20, dtype=torch.uint8, device="cuda")
+    p = nb.SimParam(numParticles=n, G=1.0, dt=DT, damping=1.0, distEps=EPS2,
+                    accumulator=nb.ACC_COMPENSATED)
+    sim = nb.Simulation(p, pos, vel, m)
+    sharded = ShardedSimulation(sim, rank, world, device="cuda")
+    first, count = sharded.shard
+    kinfo = sim.kernel_info()
+    peak_tf = nb.fp32_peak_tflops()
+    for _ in range(args.warmup):
+        sharded.step(1)
+    torch.cuda.synchronize()
+    dist.barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        for k in range(args.steps):
+            if args.flush_mib:
+                flush.zero_()
+            starts[k].record(stream)
+            sharded.step(1)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    sim.synchronize()
+    dist.barrier()
+    dev_s = max_over_ranks(sum(step_ms) / 1e3, world)
+    rate = float(n) * n * args.steps / dev_s          # the one system's pairs, whole job
+    # e2e: every rank loads the state from pinned host memory, steps (with the
+    # exchange) and reads its copy back.
+    host = [torch.empty(n, dtype=torch.float32, pin_memory=True).numpy() for _ in range(6)]
+    for h, src in zip(host, pos + vel):
+        h[:] = src
+    e2e_steps = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.set_state(host[:3], host[3:])
+        sharded.step(1)
+        sharded.gather_velocities()
+        sim.get_state(host)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    achieved_tf = FLOP_PER_PAIR * float(n) * count / (min(step_ms) * 1e-3) / 1e12
+    result = {
+        "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Plummer sphere generated by the library)",
+        "config": dict(workload_desc(n), kernel=kinfo, accumulator="compensated",
+                       parallelism=f"split{world}: i-shards of {count} particles, all-gather "
+                                   "of positions after every step",
+                       l2=(f"flushed between timed steps ({args.flush_mib} MiB write)"
+                           if args.flush_mib else "not flushed (profiling run)")),
+        "fp32_peak_frac": rate * FLOP_PER_PAIR / world / (peak_tf * 1e12),
+        "roofline": {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf,
+                     "unit": "TFLOP/s", "frac": achieved_tf / peak_tf, "traffic": None,
+                     "peak_source": "nominal: SMs x 128 FP32 lanes x 2 flop x max SM clock",
+                     "note": "per rank, this rank's shard over the whole step (all-gather "
+                             "included)"},
+        "e2e": {"value": float(n) * n * e2e_steps / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": 6 * 4 * n, "d2h_bytes_per_step": 6 * 4 * n,
+                "ms_per_step": e2e_s * 1e3 / e2e_steps},
+        "gpu_launches": args.steps, "clocks": clk.summary(),
+    }
+    sim.close()
+    return result
+
+
 def traffic_from_profile():
     """DRAM bytes per launch of the force kernel from the committed ncu summary."""
     f = ROOT / "profiles" / "force_kernel_plummer_1M.txt"
@@ -664,6 +752,10 @@ def main() -> int:
                     help="particles (default: the 1,048,576-particle workload; smaller values "
                          "are for profiling only)")
     ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--split", action="store_true",
+                    help="split the one system over the job's GPUs (strong scaling: shards of "
+                         "particles, an all-gather of positions per step) instead of running "
+                         "one replica per GPU")
     ap.add_argument("--study", choices=["precision", "accuracy", "ensemble"], default=None,
                     help="run a study instead of the benchmark (precision: config 2 over time; "
                          "accuracy: force error vs FP64 of every config, every accumulator; "
@@ -695,13 +787,22 @@ def main() -> int:
     rank, world = dist_init()
     if args.impl == "reference":
         res = run_reference(args, rank, world)
+    elif args.split:
+        res = run_split(args, rank, world)
     else:
         res = run_ours(args, rank, world)
     if rank == 0 and res is not None:
-        print(json.dumps(res), flush=True)
-    if world > 1:
-        import torch.distributed as dist
+        # Libraries below Python (NCCL announces its version on stdout) write through C
+        # stdio buffers: flush them first, so that the JSON line is the last line.
+        import ctypes
 
+        try:
+            ctypes.CDLL(None).fflush(None)
+        except (OSError, AttributeError):
+            pass
+        print(json.dumps(res), flush=True)
+    dist = sys.modules.get("torch.distributed")
+    if dist is not None and dist.is_available() and dist.is_initialized():
         dist.destroy_process_group()
     return 0
 

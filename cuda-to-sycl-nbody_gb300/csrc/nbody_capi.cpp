@@ -437,25 +437,26 @@ static int64_t reference_order_tiles(const nb_sim* s, int shape, int32_t first, 
   return tiles;
 }
 
-// Grid of the reference-order kernel: the same number of CTAs on every SM, at
-// most the occupancy limit and at most one CTA per i-tile on average, so that each
-// CTA's share is at least one whole i-tile and a hand-over chain is never longer
-// than two parts (a particle's sum is sequential: a longer chain would run its
-// parts one after another).  Fewer i-tiles than SMs: one CTA per i-tile.
+// Grid of the reference-order kernel: one CTA per i-tile while every CTA fits
+// on the GPU at once, else the occupancy limit on every SM with the stream-K work
+// list.  A CTA's share is then at least one whole i-tile, so a hand-over chain is
+// never longer than two parts (a particle's sum is sequential: a longer chain
+// would only run its parts one after another).
 static int reference_order_grid(nb_sim* s, int shape, int32_t first, int32_t count) {
   const int64_t tiles = reference_order_tiles(s, shape, first, count);
-  const int occ = max_grid_for(s, -1 - shape) / s->sms;
-  const int64_t per_sm = std::min<int64_t>(occ, tiles / s->sms);
-  return static_cast<int>(per_sm >= 1 ? per_sm * s->sms : std::max<int64_t>(1, tiles));
+  return static_cast<int>(std::max<int64_t>(
+      1, std::min<int64_t>(tiles, max_grid_for(s, -1 - shape))));
 }
 
-// Default reference-order shape: the largest i-tiles that still give every SM at
-// least two CTAs (eight warps) by reference_order_grid; the smallest shape (the
-// most particles summed at once) when none does.
+// Default reference-order shape: the largest i-tiles that still fill the GPU --
+// at least two CTAs per SM, or one where a single CTA is all that fits on an SM;
+// the smallest shape (the most particles summed at once) when none does.
 static int default_reference_order_for(nb_sim* s, int32_t first, int32_t count) {
   const int last = reference_order_num_shapes() - 1;
-  for (int k = 0; k < last; ++k)
-    if (reference_order_tiles(s, k, first, count) >= 2 * static_cast<int64_t>(s->sms)) return k;
+  for (int k = 0; k < last; ++k) {
+    const int64_t per_sm = std::min<int64_t>(2, max_grid_for(s, -1 - k) / s->sms);
+    if (reference_order_tiles(s, k, first, count) >= per_sm * s->sms) return k;
+  }
   return last;
 }
 
@@ -918,6 +919,17 @@ int nb_kernel_config_info(int32_t index, nb_kernel_info* info) {
 int nb_sim_set_kernel_config(nb_sim* s, int32_t index) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
   DeviceGuard dg_(s->device);
+  if (reference_order_mode(s)) {
+    // The reference-order kernel's shapes: index 0 .. reference-order shapes - 1.
+    if (index < -1 || index >= reference_order_num_shapes())
+      return set_error(NB_ERR_INVALID_ARGUMENT, "bad reference-order shape index");
+    const int shape =
+        index < 0 ? default_reference_order_for(s, 0, static_cast<int32_t>(s->sys_h.size()))
+                  : index;
+    NB_TRY(build_reference_order_worklist(s, shape));
+    s->ro_shape = shape;
+    return NB_OK;
+  }
   if (index < -1 || index >= num_force_configs())
     return set_error(NB_ERR_INVALID_ARGUMENT, "bad config index");
   const int cfg = index < 0 ? default_config(s) : index;

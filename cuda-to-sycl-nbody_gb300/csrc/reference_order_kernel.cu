@@ -16,7 +16,8 @@
 //     duplicated, (x, x, y, y) (z, z, m, m) per particle (ro_dup_kernel, one pass
 //     per step), so one broadcast 16-byte shared load feeds both lanes.
 //   * j-tiles of that copy are staged global -> shared by cp.async.bulk into a
-//     STAGES-deep ring with mbarrier completion, like the fast kernel.
+//     three-deep ring in dynamic shared memory with mbarrier completion, like the
+//     fast kernel.
 //   * Persistent grid with a stream-K work list (worklist.hpp): every CTA gets
 //     the same number of pair interactions to within one j-tile, whatever the
 //     number of i-tiles, so the last wave is never part-empty.  A particle's sum
@@ -35,6 +36,7 @@
 //     the reference.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 
 #include "nb_device.cuh"
@@ -44,9 +46,7 @@
 namespace nbg {
 namespace {
 
-constexpr int kRoBJ = 256;     // j-particles per shared-memory tile
 constexpr int kRoStages = 3;   // depth of the tile ring
-constexpr int kRoUnroll = 4;   // j steps per unrolled block
 constexpr uint64_t kRoWaitNs = 2000000000ull;
 
 __device__ __forceinline__ uint32_t ro_smem_u32(const void* p) {
@@ -179,7 +179,7 @@ __device__ __forceinline__ void ro_step(const float4 xy, const float4 zm, float2
 }
 
 // Steps over j = j0 .. j0 + count - 1 of the staged tile, in order.
-template <int P, bool kDiag>
+template <int P, bool kDiag, int kRoUnroll>
 __device__ __forceinline__ void ro_tile(const float4* __restrict__ tile, int count, int j0,
                                         float2 e2, const float2 (&nx)[P], const float2 (&ny)[P],
                                         const float2 (&nz)[P], float2 (&ax)[P], float2 (&ay)[P],
@@ -211,12 +211,16 @@ __global__ void ro_dup_kernel(const float4* __restrict__ pos4, int64_t records,
   }
 }
 
-template <int THREADS, int P>
-__global__ void __launch_bounds__(THREADS) reference_order_kernel(const ForceArgs a,
-                                                                  const float4* __restrict__ dup) {
+// THREADS threads x P i-pairs per thread (i-tiles of 2 P THREADS particles), j-tiles
+// of BJ particles (the ring holds kRoStages of them, BJ x 32 bytes each), U j steps
+// per unrolled block, registers budgeted for MINB resident CTAs per SM.
+template <int THREADS, int P, int BJ, int U, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) reference_order_kernel(
+    const ForceArgs a, const float4* __restrict__ dup) {
   constexpr int BI = THREADS * 2 * P;  // i-particles per i-tile
   static_assert(BI % kPadQuantum == 0, "i-tiles must hold whole padding quanta");
-  __shared__ __align__(128) float4 ring[kRoStages][kRoBJ * 2];
+  extern __shared__ __align__(128) float4 ring_smem[];  // [kRoStages][BJ * 2]
+  auto ring = [&](uint32_t slot) { return ring_smem + slot * (BJ * 2); };
   __shared__ __align__(8) uint64_t full_bar[kRoStages];
   __shared__ int s_bail;
 
@@ -241,15 +245,15 @@ __global__ void __launch_bounds__(THREADS) reference_order_kernel(const ForceArg
     if (p_seg < seg_lo) return;
     const Segment& sg = a.segs[p_seg];
     const SystemDesc& sd = a.sys[sg.sys];
-    const int count = min(kRoBJ, sd.n - p_jt * kRoBJ);
-    const int64_t first = sd.offset + static_cast<int64_t>(p_jt) * kRoBJ;
+    const int count = min(BJ, sd.n - p_jt * BJ);
+    const int64_t first = sd.offset + static_cast<int64_t>(p_jt) * BJ;
     const uint32_t slot = issued % kRoStages;
     // Failure-detection test: leave the first tile's barrier without arrival or
     // copy, so the consumers' bounded wait on it runs out.
     if (!(a.skip_first_tile && issued == 0)) {
       ro_fence_proxy_async();
       ro_arrive_expect_tx(&full_bar[slot], static_cast<uint32_t>(count) * 32u);
-      ro_bulk_g2s(&ring[slot][0], dup + 2 * first, static_cast<uint32_t>(count) * 32u,
+      ro_bulk_g2s(ring(slot), dup + 2 * first, static_cast<uint32_t>(count) * 32u,
                   &full_bar[slot]);
     }
     ++issued;
@@ -327,14 +331,14 @@ __global__ void __launch_bounds__(THREADS) reference_order_kernel(const ForceArg
       if (tid == 0) produce();
       const uint32_t slot = consumed % kRoStages;
       if (!ro_wait(&full_bar[slot], (consumed / kRoStages) & 1u)) timed_out = true;
-      const int j0 = jt * kRoBJ;
-      const int count = min(kRoBJ, sd.n - j0);
+      const int j0 = jt * BJ;
+      const int count = min(BJ, sd.n - j0);
       const bool diag = (j0 < ibase + BI) && (ibase < j0 + count);
       if (!timed_out) {
         if (diag)
-          ro_tile<P, true>(ring[slot], count, j0, e2, nx, ny, nz, ax, ay, az, li);
+          ro_tile<P, true, U>(ring(slot), count, j0, e2, nx, ny, nz, ax, ay, az, li);
         else
-          ro_tile<P, false>(ring[slot], count, j0, e2, nx, ny, nz, ax, ay, az, li);
+          ro_tile<P, false, U>(ring(slot), count, j0, e2, nx, ny, nz, ax, ay, az, li);
       }
       if (__syncthreads_or(timed_out)) {
         bail();
@@ -373,16 +377,44 @@ __global__ void __launch_bounds__(THREADS) reference_order_kernel(const ForceArg
 struct RoShapeEntry {
   int threads;
   int pairs;
+  int bj;
   void (*kernel)(const ForceArgs, const float4*);
 };
 
-// Largest i-tiles first.
+#define RO_SHAPE(T, P, BJ, U, B) {T, P, BJ, reference_order_kernel<T, P, BJ, U, B>}
+// Largest i-tiles first.  Measured at N = 1M (fraction of nominal FP32 peak, one
+// launch): 384 x 2 with 1024-particle j-tiles 69.8 % (12 warps, one CTA per SM);
+// 384 x 2 x 256 69.0 %; 512 x 2 67.9 % (16 warps, 128 registers); 256 x 2 66.5 %
+// (8 warps); 128 x 4 65.9 %; 128 x 2 64.2 %; 448 x 2 and 320 x 2 (warps not a
+// multiple of the SM's four schedulers) 59 %; 64 x 1 53.4 %.  The small shapes
+// serve systems too small to fill the GPU with the large i-tiles.
 const RoShapeEntry kRoShapes[] = {
-    {128, 4, reference_order_kernel<128, 4>},
-    {128, 2, reference_order_kernel<128, 2>},
-    {64, 1, reference_order_kernel<64, 1>},
+    RO_SHAPE(384, 2, 1024, 4, 1),
+    RO_SHAPE(128, 2, 256, 4, 1),
+    RO_SHAPE(64, 1, 256, 4, 1),
 };
 constexpr int kNumRoShapes = sizeof(kRoShapes) / sizeof(kRoShapes[0]);
+
+size_t ro_smem_bytes(const RoShapeEntry& e) {
+  return static_cast<size_t>(kRoStages) * e.bj * 32;
+}
+
+// Rings of 48 KB or more opt in to the larger dynamic shared memory, once per
+// device ordinal and shape (ordinals >= 64 opt in on every call).
+cudaError_t ro_smem_opt_in(int index) {
+  static std::atomic<uint64_t> opted[kNumRoShapes];
+  const RoShapeEntry& e = kRoShapes[index];
+  if (ro_smem_bytes(e) < 48 * 1024) return cudaSuccess;
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  const uint64_t bit = dev >= 0 && dev < 64 ? uint64_t{1} << dev : 0;
+  if (bit != 0 && (opted[index].load(std::memory_order_acquire) & bit) != 0) return cudaSuccess;
+  err = cudaFuncSetAttribute(e.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(ro_smem_bytes(e)));
+  if (err == cudaSuccess && bit != 0) opted[index].fetch_or(bit, std::memory_order_release);
+  return err;
+}
 
 }  // namespace
 
@@ -390,12 +422,15 @@ int reference_order_num_shapes() { return kNumRoShapes; }
 
 KernelShape reference_order_shape(int index) {
   const RoShapeEntry& e = kRoShapes[index];
-  return KernelShape{e.threads, 2 * e.pairs, kRoBJ, kRoStages};
+  return KernelShape{e.threads, 2 * e.pairs, e.bj, kRoStages};
 }
 
 cudaError_t reference_order_blocks_per_sm(int index, int* blocks) {
   const RoShapeEntry& e = kRoShapes[index];
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, e.kernel, e.threads, 0);
+  const cudaError_t err = ro_smem_opt_in(index);
+  if (err != cudaSuccess) return err;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, e.kernel, e.threads,
+                                                       ro_smem_bytes(e));
 }
 
 cudaError_t launch_reference_order_dup(const float* pos, int64_t n_pad_total, float4* dup,
@@ -411,6 +446,8 @@ cudaError_t launch_reference_order_dup(const float* pos, int64_t n_pad_total, fl
 cudaError_t launch_reference_order(int index, const ForceArgs& a, const float4* dup, int grid,
                                    cudaStream_t stream) {
   const RoShapeEntry& e = kRoShapes[index];
+  const cudaError_t err = ro_smem_opt_in(index);
+  if (err != cudaSuccess) return err;
   // Cooperative: every CTA is resident, so a CTA waiting for its predecessor's
   // hand-over always waits on a running CTA.
   cudaLaunchAttribute attr[1];
@@ -419,7 +456,7 @@ cudaError_t launch_reference_order(int index, const ForceArgs& a, const float4* 
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(e.threads);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = ro_smem_bytes(e);
   cfg.stream = stream;
   cfg.attrs = attr;
   cfg.numAttrs = 1;

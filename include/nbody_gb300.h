@@ -262,7 +262,9 @@ int nb_sim_load_state_block(nb_sim* s, uint64_t first, uint64_t count, int32_t w
  * and gwSize is only reported here (nb_sim_gw_size). */
 int nb_num_kernel_configs(void);
 int nb_kernel_config_info(int32_t index, nb_kernel_info* info);
-/* Select a kernel shape by index (-1 = the built-in default for this size). */
+/* Select a kernel shape by index (-1 = the built-in default for this size).  With
+ * NB_ACC_REFERENCE_ORDER the index selects one of the reference-order kernel's
+ * shapes (0 = the largest i-tiles; nb_sim_kernel_info reports it as -1 - index). */
 int nb_sim_set_kernel_config(nb_sim* s, int32_t index);
 int nb_sim_kernel_info(const nb_sim* s, nb_kernel_info* info);
 /* Time every kernel shape on this simulation's data (accelerations only, the

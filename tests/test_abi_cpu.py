@@ -308,3 +308,28 @@ def test_null_handles_are_rejected_without_touching_the_device():
     assert L.nb_accelerations_noalloc(None, 1, 1.0, 1e-3, None, None) == \
         nb.NB_ERR_INVALID_ARGUMENT
     assert "NULL" in L.nb_last_error().decode()
+
+
+@pytest.mark.parametrize("n,cfg,grid", [(1 << 20, 1, 152), (1 << 20, 1, 456), (262144, 0, 152),
+                                        (262144, 0, 456), (300000, 1, 152), (25600, 3, 50)])
+def test_ordered_hand_over_schedule_never_waits(n, cfg, grid):
+    """The reference-order kernel's schedule, replayed on the work-list planner with
+    unit cost per j-tile: each CTA walks its segments last to first, and the part of
+    a split i-tile may start only when the previous part has finished.  With at most
+    one CTA per i-tile (the kernel's grid rule) no part waits and no i-tile is split
+    into more than two parts."""
+    info = nb.kernel_config_info(cfg)
+    bi = info["threads_per_block"] * info["particles_per_thread"]
+    assert grid <= -(-n // bi)
+    g, segs, begin, nfix, slots = nb.plan_work([n], cfg, grid)
+    finish = {}
+    for c in range(g):
+        t = 0
+        for q in range(begin[c + 1] - 1, begin[c] - 1, -1):
+            _, _, j0, j1, fix, part = segs[q]
+            if fix >= 0 and part > 0:
+                assert finish[(fix, part - 1)] <= t, (c, fix, part)
+            t += j1 - j0
+            if fix >= 0:
+                finish[(fix, part)] = t
+    assert all(part <= 1 for *_, part in segs)

@@ -19,7 +19,7 @@ def test_bench_json_contract_small_case():
                         "--warmup", "3", "--no-extras", "--no-cpu"],
                        capture_output=True, text=True, timeout=600, cwd=str(ROOT))
     assert r.returncode == 0, r.stderr[-2000:]
-    d = json.loads(r.stdout.strip().splitlines()[-1])
+    d = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
                 "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
                 "roofline", "e2e", "gpu_launches", "clocks", "accumulators"):
@@ -38,3 +38,18 @@ def test_bench_json_contract_small_case():
     assert set(d["accumulators"]) == {"plain", "compensated", "reference_order"}
     assert d["config"]["accumulator"] in d["accumulators"]
     assert d["clocks"]["samples"] >= 0
+
+
+def test_bench_split_mode_small_case():
+    # --split: the one system over the job's GPUs (here a one-rank NCCL group);
+    # the timed step includes the all-gather of positions.
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--split", "--n", "65536",
+                        "--steps", "3", "--warmup", "3", "--no-extras", "--no-cpu"],
+                       capture_output=True, text=True, timeout=600, cwd=str(ROOT))
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip().splitlines()[-1].startswith("{")   # the JSON line comes last
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    assert d["scaling"] == "strong" and d["n_gpus"] == 1
+    assert d["config"]["parallelism"].startswith("split1")
+    assert d["value"] == pytest.approx(65536.0 ** 2 / (d["ms_per_step"] * 1e-3), rel=1e-6)
+    assert d["e2e"]["value"] > 0 and d["gpu_launches"] == 3

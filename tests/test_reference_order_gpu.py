@@ -213,9 +213,9 @@ def test_thousand_steps_bitwise_equal_to_reference_kernel():
 @needs_reference
 @pytest.mark.parametrize("n", [25600, 300000, 1 << 20])
 def test_every_shape_and_autotune_stay_bitwise(n):
-    """The default shape depends on the size: the largest i-tiles that still give
-    every SM two CTAs (the stream-K grid hands split i-tiles over between CTAs);
-    the autotuner picks among all shapes; every choice gives the reference's bits."""
+    """The default shape depends on the size: the largest i-tiles that still fill the
+    GPU (the stream-K grid hands split i-tiles over between CTAs); the autotuner
+    picks among all shapes; every choice gives the reference's bits."""
     pos, vel, _ = disk_case(n, seed=31)
     G = float(np.float32(1.0 / n))
     ref, _ = orc.reference_run(pos, vel, G, 1e-3, 0.999, 1e-3, iters=2, method=orc.BRANCH)
@@ -229,9 +229,7 @@ def test_every_shape_and_autotune_stay_bitwise(n):
         got = sim.get_state()
     assert default <= -1
     if n == 25600:
-        assert default == -3          # 64 x 1: 200 i-tiles (128 x 4 would give 25)
-    elif n == 300000:
-        assert default == -2          # 128 x 2: 586 i-tiles (128 x 4: 293 < 2 x 152 SMs)
+        assert default == -3          # 64 x 1: 200 i-tiles (384 x 2 would give 34)
     else:
-        assert default == -1          # 128 x 4: 1024 i-tiles
+        assert default == -1          # 384 x 2: 391 (n = 300,000) or 1366 i-tiles
     assert same_bits(got, ref)

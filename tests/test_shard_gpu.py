@@ -97,7 +97,8 @@ def test_shard_arguments_and_what_they_invalidate():
         assert sim.state_block_bytes(992, 8) == 16 * 16
         with pytest.raises(nb.NbError):
             sim.copy_state_block(0, 16, 3, 1)         # unknown block kind
-        sim.set_stream(torch.cuda.current_stream().cuda_stream)
+        side = torch.cuda.Stream()                    # graphs are captured on a non-default stream
+        sim.set_stream(side.cuda_stream)
         sim.graph_capture(2)
         sim.set_shard(0, 512)                         # new work list: the graph is dropped
         with pytest.raises(nb.NbError) as e:
