@@ -685,6 +685,32 @@ def run_accuracy_study(args) -> dict:
     return out
 
 
+# --------------------------------------------------------------------------- sizes study
+def run_sizes_study(args) -> dict:
+    """ms per step of the tuned kernel (compensated, default shape) and of the
+    reference-order kernel (default shape) from N = 2,048 to 1,048,576 (config-0
+    style thin disks, eps2 = 1e-3), CUDA events, median of repeated launches."""
+    import nbody_gb300 as nb
+
+    out = {"study": "sizes", "eps2": 1e-3, "cases": {}}
+    for n in (2048, 25600, 65536, 262144, 1 << 20):
+        (x, y, z), (vx, vy, vz), m = nb.thin_disk(SEED, n, 1e-3)
+        row = {}
+        for name, acc in (("compensated", nb.ACC_COMPENSATED),
+                          ("reference_order", nb.ACC_REFERENCE_ORDER)):
+            p = nb.SimParam(numParticles=n, G=1.0, dt=1e-3, damping=1.0, distEps=1e-3,
+                            accumulator=acc)
+            with nb.Simulation(p, (x, y, z), (vx, vy, vz), m) as sim:
+                reps = 20 if n <= 65536 else (5 if n <= 262144 else 3)
+                sim.advance(2)
+                times = [sim.time_iterations(1) for _ in range(reps)]
+                row[name] = {"ms_per_step": statistics.median(times),
+                             "pairs_per_s": float(n) * n / (statistics.median(times) * 1e-3),
+                             "kernel": sim.kernel_info()}
+        out["cases"][str(n)] = row
+    return out
+
+
 # --------------------------------------------------------------------------- reference arm
 def run_reference(args, rank, world) -> dict | None:
     if rank != 0:
@@ -756,10 +782,12 @@ def main() -> int:
                     help="split the one system over the job's GPUs (strong scaling: shards of "
                          "particles, an all-gather of positions per step) instead of running "
                          "one replica per GPU")
-    ap.add_argument("--study", choices=["precision", "accuracy", "ensemble"], default=None,
+    ap.add_argument("--study", choices=["precision", "accuracy", "ensemble", "sizes"],
+                    default=None,
                     help="run a study instead of the benchmark (precision: config 2 over time; "
                          "accuracy: force error vs FP64 of every config, every accumulator; "
-                         "ensemble: the 4,096-system ensemble leg alone, for profiling)")
+                         "ensemble: the 4,096-system ensemble leg alone, for profiling; "
+                         "sizes: both kernels from N = 2,048 to 1M)")
     ap.add_argument("--study-steps", type=int, default=1000)
     ap.add_argument("--flush-mib", type=int, default=512,
                     help="L2 flush buffer written between timed steps (0: no flush; profiling)")
@@ -783,6 +811,9 @@ def main() -> int:
         return 0
     if args.study == "ensemble":
         print(json.dumps(bench_ensemble(args)), flush=True)
+        return 0
+    if args.study == "sizes":
+        print(json.dumps(run_sizes_study(args)), flush=True)
         return 0
     rank, world = dist_init()
     if args.impl == "reference":
