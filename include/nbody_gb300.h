@@ -240,7 +240,8 @@ typedef enum nb_block_kind { NB_BLOCK_POSITIONS = 1, NB_BLOCK_VELOCITIES = 2 } n
  * [first, first + count): their next positions and velocities are written, the
  * others' are not.  first is a multiple of 16, and so is count unless the shard
  * ends the system; count = 0 restores the whole system.  Drops any captured graph;
- * the adjoint needs the whole system.  BRANCH method only. */
+ * the adjoint needs the whole system.  nb_sim_accelerations then computes only the
+ * shard's rows (the other rows it returns are unspecified).  BRANCH method only. */
 int nb_sim_set_shard(nb_sim* s, uint64_t first, uint64_t count);
 /* Size in bytes of the state block of particles [first, first + count) (16 bytes per
  * particle; a block that ends the system is padded to a multiple of 16 particles). */
