@@ -687,19 +687,21 @@ def run_accuracy_study(args) -> dict:
 
 # --------------------------------------------------------------------------- sizes study
 def run_sizes_study(args) -> dict:
-    """ms per step of the tuned kernel (compensated, default shape) and of the
-    reference-order kernel (default shape) from N = 2,048 to 1,048,576 (config-0
-    style thin disks, eps2 = 1e-3), CUDA events, median of repeated launches."""
+    """ms per step of the tuned kernel (compensated, default shape), of the
+    reference-order kernel (default shape) and of the PREDICATED compatibility kernel
+    from N = 2,048 to 1,048,576 (config-0 style thin disks, eps2 = 1e-3), CUDA events,
+    median of repeated launches."""
     import nbody_gb300 as nb
 
     out = {"study": "sizes", "eps2": 1e-3, "cases": {}}
     for n in (2048, 25600, 65536, 262144, 1 << 20):
         (x, y, z), (vx, vy, vz), m = nb.thin_disk(SEED, n, 1e-3)
         row = {}
-        for name, acc in (("compensated", nb.ACC_COMPENSATED),
-                          ("reference_order", nb.ACC_REFERENCE_ORDER)):
+        for name, acc, method in (("compensated", nb.ACC_COMPENSATED, nb.BRANCH),
+                                  ("reference_order", nb.ACC_REFERENCE_ORDER, nb.BRANCH),
+                                  ("predicated", nb.ACC_COMPENSATED, nb.PREDICATED)):
             p = nb.SimParam(numParticles=n, G=1.0, dt=1e-3, damping=1.0, distEps=1e-3,
-                            accumulator=acc)
+                            accumulator=acc, calcMethod=method)
             with nb.Simulation(p, (x, y, z), (vx, vy, vz), m) as sim:
                 reps = 20 if n <= 65536 else (5 if n <= 262144 else 3)
                 sim.advance(2)

@@ -129,7 +129,9 @@ __device__ __noinline__ bool ro_wait_counter(const int32_t* counter, int32_t tar
 // One j step against all of the thread's i-pairs.  kDiag: the tile overlaps the
 // i-tile, so the term of j == i is left out of that lane's sum (the reference's
 // `if (i == id) continue;`), by keeping the old value rather than adding zero.
-template <int P, bool kDiag>
+// kPred: the PREDICATED variant as shipped, force += r * inv * (j == i)
+// (simulator.cu:209), contracted to fma(r * inv, mask, force) for every j.
+template <int P, bool kDiag, bool kPred>
 __device__ __forceinline__ void ro_step(const float4 xy, const float4 zm, float2 e2,
                                         const float2 (&nx)[P], const float2 (&ny)[P],
                                         const float2 (&nz)[P], float2 (&ax)[P],
@@ -156,6 +158,14 @@ __device__ __forceinline__ void ro_step(const float4 xy, const float4 zm, float2
     float2 t = __fmul2_rn(d2, d2);
     t = __fmul2_rn(t, d2);
     const float2 inv = make_float2(rsqrtf(t.x), rsqrtf(t.y));
+    if (kPred) {
+      const float2 mask = kDiag ? make_float2(j == li[k] ? 1.f : 0.f, j == li[k] + 1 ? 1.f : 0.f)
+                                : make_float2(0.f, 0.f);
+      ax[k] = __ffma2_rn(__fmul2_rn(rx, inv), mask, ax[k]);
+      ay[k] = __ffma2_rn(__fmul2_rn(ry, inv), mask, ay[k]);
+      az[k] = __ffma2_rn(__fmul2_rn(rz, inv), mask, az[k]);
+      continue;
+    }
     // force += r * inv (:206), contracted
     float2 fx = __ffma2_rn(rx, inv, ax[k]);
     float2 fy = __ffma2_rn(ry, inv, ay[k]);
@@ -179,7 +189,7 @@ __device__ __forceinline__ void ro_step(const float4 xy, const float4 zm, float2
 }
 
 // Steps over j = j0 .. j0 + count - 1 of the staged tile, in order.
-template <int P, bool kDiag, int kRoUnroll>
+template <int P, bool kDiag, bool kPred, int kRoUnroll>
 __device__ __forceinline__ void ro_tile(const float4* __restrict__ tile, int count, int j0,
                                         float2 e2, const float2 (&nx)[P], const float2 (&ny)[P],
                                         const float2 (&nz)[P], float2 (&ax)[P], float2 (&ay)[P],
@@ -189,12 +199,12 @@ __device__ __forceinline__ void ro_tile(const float4* __restrict__ tile, int cou
   for (; jj + kRoUnroll <= count; jj += kRoUnroll) {
 #pragma unroll
     for (int u = 0; u < kRoUnroll; ++u)
-      ro_step<P, kDiag>(tile[2 * (jj + u)], tile[2 * (jj + u) + 1], e2, nx, ny, nz, ax, ay, az,
+      ro_step<P, kDiag, kPred>(tile[2 * (jj + u)], tile[2 * (jj + u) + 1], e2, nx, ny, nz, ax, ay, az,
                         j0 + jj + u, li);
   }
 #pragma unroll 1
   for (; jj < count; ++jj)
-    ro_step<P, kDiag>(tile[2 * jj], tile[2 * jj + 1], e2, nx, ny, nz, ax, ay, az, j0 + jj, li);
+    ro_step<P, kDiag, kPred>(tile[2 * jj], tile[2 * jj + 1], e2, nx, ny, nz, ax, ay, az, j0 + jj, li);
 }
 
 // The duplicated j-layout from the pair layout: one thread per pair record.
@@ -213,8 +223,9 @@ __global__ void ro_dup_kernel(const float4* __restrict__ pos4, int64_t records,
 
 // THREADS threads x P i-pairs per thread (i-tiles of 2 P THREADS particles), j-tiles
 // of BJ particles (the ring holds kRoStages of them, BJ x 32 bytes each), U j steps
-// per unrolled block, registers budgeted for MINB resident CTAs per SM.
-template <int THREADS, int P, int BJ, int U, int MINB>
+// per unrolled block, registers budgeted for MINB resident CTAs per SM; kPred: the
+// PREDICATED variant's pair term (ro_step).
+template <int THREADS, int P, int BJ, int U, int MINB, bool kPred>
 __global__ void __launch_bounds__(THREADS, MINB) reference_order_kernel(
     const ForceArgs a, const float4* __restrict__ dup) {
   constexpr int BI = THREADS * 2 * P;  // i-particles per i-tile
@@ -336,9 +347,9 @@ __global__ void __launch_bounds__(THREADS, MINB) reference_order_kernel(
       const bool diag = (j0 < ibase + BI) && (ibase < j0 + count);
       if (!timed_out) {
         if (diag)
-          ro_tile<P, true, U>(ring(slot), count, j0, e2, nx, ny, nz, ax, ay, az, li);
+          ro_tile<P, true, kPred, U>(ring(slot), count, j0, e2, nx, ny, nz, ax, ay, az, li);
         else
-          ro_tile<P, false, U>(ring(slot), count, j0, e2, nx, ny, nz, ax, ay, az, li);
+          ro_tile<P, false, kPred, U>(ring(slot), count, j0, e2, nx, ny, nz, ax, ay, az, li);
       }
       if (__syncthreads_or(timed_out)) {
         bail();
@@ -378,10 +389,12 @@ struct RoShapeEntry {
   int threads;
   int pairs;
   int bj;
-  void (*kernel)(const ForceArgs, const float4*);
+  void (*kernel[2])(const ForceArgs, const float4*);  // [BRANCH, PREDICATED]
 };
 
-#define RO_SHAPE(T, P, BJ, U, B) {T, P, BJ, reference_order_kernel<T, P, BJ, U, B>}
+#define RO_SHAPE(T, P, BJ, U, B)                                                   \
+  {T, P, BJ, {reference_order_kernel<T, P, BJ, U, B, false>,                       \
+              reference_order_kernel<T, P, BJ, U, B, true>}}
 // Largest i-tiles first.  Measured at N = 1M (fraction of nominal FP32 peak, one
 // launch): 384 x 2 with 1024-particle j-tiles 69.8 % (12 warps, one CTA per SM);
 // 384 x 2 x 256 69.0 %; 512 x 2 67.9 % (16 warps, 128 registers); 256 x 2 66.5 %

@@ -289,7 +289,10 @@ int nb_plan_work(uint32_t num_systems, const uint32_t* sizes, int32_t config_ind
 /* ---- CUDA graphs ------------------------------------------------------------------ */
 /* No reference counterpart: stepSim launches every iteration itself
  * (simulator.cu:57-66). */
-/* Capture `iterations` iterations into a CUDA graph (replacing any earlier one). */
+/* Capture `iterations` iterations into a CUDA graph (replacing any earlier one).
+ * The graph holds the current work list's device addresses: choosing another
+ * kernel shape (nb_sim_set_kernel_config, nb_sim_autotune) or shard drops it, and
+ * nb_sim_graph_launch then returns NB_ERR_STATE until the next capture. */
 int nb_sim_graph_capture(nb_sim* s, int32_t iterations);
 /* Launch the captured graph once on the simulation's stream. */
 int nb_sim_graph_launch(nb_sim* s);
