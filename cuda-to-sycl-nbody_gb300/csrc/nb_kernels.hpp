@@ -24,7 +24,8 @@ cudaError_t launch_predicated(const ForceArgs& a, const SystemDesc& sd, int32_t 
 
 // ---- reference-order force + integrate (reference_order_kernel.cu) -------------------
 // particle_interaction<BRANCH> with the reference's per-particle summation order
-// and arithmetic (bit-identical results on the same GPU), equal masses per system.
+// and arithmetic (bit-identical results on the same GPU), equal masses per system;
+// `predicated` selects particle_interaction<PREDICATED>'s pair term instead.
 // Shapes are indexed largest i-tile first.  The kernel walks a stream-K work list
 // (ForceArgs segs / seg_begin / fix) of reference_order_shape(index) tiles; split
 // i-tiles hand their running sums over through `partials` and `counters`.  `dup` is
@@ -32,11 +33,11 @@ cudaError_t launch_predicated(const ForceArgs& a, const SystemDesc& sd, int32_t 
 // launch_reference_order_dup.  The launch is cooperative: grid <= blocks per SM x SMs.
 int reference_order_num_shapes();
 KernelShape reference_order_shape(int index);  // threads, i-particles per thread, j-tile, stages
-cudaError_t reference_order_blocks_per_sm(int index, int* blocks);
+cudaError_t reference_order_blocks_per_sm(int index, bool predicated, int* blocks);
 cudaError_t launch_reference_order_dup(const float* pos, int64_t n_pad_total, float4* dup,
                                        cudaStream_t stream);
-cudaError_t launch_reference_order(int index, const ForceArgs& a, const float4* dup, int grid,
-                                   cudaStream_t stream);
+cudaError_t launch_reference_order(int index, bool predicated, const ForceArgs& a,
+                                   const float4* dup, int grid, cudaStream_t stream);
 
 // ---- measured FP32 throughput (peak_probe.cu) ----------------------------------------
 // Time `repeats` launches (after one warm-up) of an FFMA2 loop over sms x blocks_per_sm

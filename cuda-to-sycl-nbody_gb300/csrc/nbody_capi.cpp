@@ -207,9 +207,10 @@ static int ensure_scratch(nb_sim* s, const WorkListDev& w) {
 static int max_grid_for(nb_sim* s, int cfg) {
   int blocks = 0;
   const bool comp = s->params.accumulator == NB_ACC_COMPENSATED;
-  const cudaError_t e = cfg >= 0
-                            ? force_blocks_per_sm(cfg, comp, s->per_pair_mass, &blocks)
-                            : reference_order_blocks_per_sm(-1 - cfg, &blocks);
+  const cudaError_t e =
+      cfg >= 0 ? force_blocks_per_sm(cfg, comp, s->per_pair_mass, &blocks)
+               : reference_order_blocks_per_sm(-1 - cfg, s->params.calc_method == NB_PREDICATED,
+                                               &blocks);
   if (e != cudaSuccess || blocks < 1) blocks = 1;
   return blocks * s->sms;
 }
@@ -271,6 +272,14 @@ static bool reference_order_mode(const nb_sim* s) {
   return s->params.calc_method == NB_BRANCH && s->params.accumulator == NB_ACC_REFERENCE_ORDER;
 }
 
+// The modes that run the sequential-order kernel (reference_order_kernel.cu): the
+// reference-order accumulator, and PREDICATED, whose equal-mass systems run that
+// kernel with the PREDICATED pair term (per-particle masses keep the one-thread-
+// per-particle kernel, aux_kernels.cu).
+static bool sequential_order_mode(const nb_sim* s) {
+  return reference_order_mode(s) || s->params.calc_method == NB_PREDICATED;
+}
+
 // (Re)build the reference-order work list for shape `shape` (all systems).
 static int reference_order_grid(nb_sim* s, int shape, int32_t first, int32_t count);
 
@@ -294,7 +303,7 @@ static int build_reference_order_worklist(nb_sim* s, int shape) {
 // way a caller launching each system separately would; kPerSystemSimShape gives
 // every system the simulation's current shape.
 static int build_per_system_worklists(nb_sim* s, int policy) {
-  const bool ro = reference_order_mode(s);
+  const bool ro = sequential_order_mode(s);
   const int sim_cfg = ro ? -1 - s->ro_shape : s->cfg;
   if (s->wl_sys_policy == policy && (policy == kPerSystemOwnShape || s->wl_sys_cfg == sim_cfg) &&
       s->wl_sys.size() == s->sys_h.size())
@@ -349,8 +358,9 @@ int launch_with(nb_sim* s, ForceArgs a, const WorkListDev& w) {
   a.seg_begin = w.seg_begin;
   a.fix = w.fix;
   if (w.cfg < 0) {
-    // Reference order: the duplicated layout of a.pos must have been written.
-    NB_CUDA(launch_reference_order(-1 - w.cfg, a, s->ro_dup_d, w.grid, s->stream));
+    // Sequential order: the duplicated layout of a.pos must have been written.
+    NB_CUDA(launch_reference_order(-1 - w.cfg, s->params.calc_method == NB_PREDICATED, a,
+                                   s->ro_dup_d, w.grid, s->stream));
     return NB_OK;
   }
   NB_CUDA(launch_force(w.cfg, s->params.accumulator == NB_ACC_COMPENSATED, s->per_pair_mass, a,
@@ -363,10 +373,10 @@ int launch_with(nb_sim* s, ForceArgs a, const WorkListDev& w) {
 int force_pass(nb_sim* s, float4* accel_out, int per_system) {
   ForceArgs a = base_args(s);
   a.accel_out = accel_out;
-  if (s->params.calc_method == NB_PREDICATED) {
+  if (s->params.calc_method == NB_PREDICATED && s->per_pair_mass) {
     for (int32_t k = 0; k < static_cast<int32_t>(s->sys_h.size()); ++k)
       NB_CUDA(launch_predicated(a, s->sys_h[k], k, s->stream));
-  } else if (s->params.accumulator == NB_ACC_REFERENCE_ORDER) {
+  } else if (sequential_order_mode(s)) {
     if (s->per_pair_mass) return set_error(NB_ERR_INVALID_ARGUMENT, kReferenceOrderMassError);
     NB_TRY(ensure_reference_order_dup(s));
     NB_CUDA(launch_reference_order_dup(a.pos, s->n_pad, s->ro_dup_d, s->stream));
@@ -559,7 +569,7 @@ static int create_impl(const nb_params* p, uint32_t num_systems, const uint32_t*
     return fail(cuda_error(e, "copy state"));
   s->cfg = default_config(s);
   if ((st = build_main_worklist(s, s->cfg)) != NB_OK) return fail(st);
-  if (reference_order_mode(s)) {
+  if (sequential_order_mode(s)) {
     s->ro_shape = default_reference_order_for(s, 0, static_cast<int32_t>(s->sys_h.size()));
     if ((st = build_reference_order_worklist(s, s->ro_shape)) != NB_OK) return fail(st);
     if ((st = ensure_reference_order_dup(s)) != NB_OK) return fail(st);
@@ -919,7 +929,7 @@ int nb_kernel_config_info(int32_t index, nb_kernel_info* info) {
 int nb_sim_set_kernel_config(nb_sim* s, int32_t index) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
   DeviceGuard dg_(s->device);
-  if (reference_order_mode(s)) {
+  if (sequential_order_mode(s)) {
     // The reference-order kernel's shapes: index 0 .. reference-order shapes - 1.
     if (index < -1 || index >= reference_order_num_shapes())
       return set_error(NB_ERR_INVALID_ARGUMENT, "bad reference-order shape index");
@@ -940,7 +950,7 @@ int nb_sim_set_kernel_config(nb_sim* s, int32_t index) {
 
 int nb_sim_kernel_info(const nb_sim* s, nb_kernel_info* info) {
   if (!s || !info) return set_error(NB_ERR_INVALID_ARGUMENT, "NULL argument");
-  if (reference_order_mode(s)) {
+  if (sequential_order_mode(s)) {
     const KernelShape sh = reference_order_shape(s->ro_shape);
     *info = nb_kernel_info{-1 - s->ro_shape, sh.threads, sh.r, sh.bj, sh.stages,
                            s->ro_wl.grid, s->ro_wl.nseg, s->ro_wl.split};
@@ -956,8 +966,8 @@ int nb_sim_autotune(nb_sim* s, int32_t* chosen) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
   DeviceGuard dg_(s->device);
   if (s->params.calc_method == NB_PREDICATED) {
-    // The compatibility kernel has one fixed shape: nothing to choose.
-    if (chosen) *chosen = s->cfg;
+    // The compatibility mode keeps its default shape: nothing to choose.
+    if (chosen) *chosen = -1 - s->ro_shape;
     return NB_OK;
   }
   NB_TRY(ensure_accel(s));
@@ -1192,7 +1202,7 @@ int nb_sim_inject_wait_timeout(nb_sim* s) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
   DeviceGuard dg_(s->device);
   if (s->params.calc_method != NB_BRANCH)
-    return set_error(NB_ERR_STATE, "the PREDICATED kernel has no device-side waits");
+    return set_error(NB_ERR_STATE, "the wait-timeout hook covers the BRANCH kernels only");
   s->inject_timeout = 1;
   return NB_OK;
 }

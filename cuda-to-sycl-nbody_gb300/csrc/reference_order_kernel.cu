@@ -423,8 +423,9 @@ cudaError_t ro_smem_opt_in(int index) {
   if (err != cudaSuccess) return err;
   const uint64_t bit = dev >= 0 && dev < 64 ? uint64_t{1} << dev : 0;
   if (bit != 0 && (opted[index].load(std::memory_order_acquire) & bit) != 0) return cudaSuccess;
-  err = cudaFuncSetAttribute(e.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(ro_smem_bytes(e)));
+  for (int v = 0; v < 2 && err == cudaSuccess; ++v)
+    err = cudaFuncSetAttribute(e.kernel[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(ro_smem_bytes(e)));
   if (err == cudaSuccess && bit != 0) opted[index].fetch_or(bit, std::memory_order_release);
   return err;
 }
@@ -438,11 +439,11 @@ KernelShape reference_order_shape(int index) {
   return KernelShape{e.threads, 2 * e.pairs, e.bj, kRoStages};
 }
 
-cudaError_t reference_order_blocks_per_sm(int index, int* blocks) {
+cudaError_t reference_order_blocks_per_sm(int index, bool predicated, int* blocks) {
   const RoShapeEntry& e = kRoShapes[index];
   const cudaError_t err = ro_smem_opt_in(index);
   if (err != cudaSuccess) return err;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, e.kernel, e.threads,
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, e.kernel[predicated], e.threads,
                                                        ro_smem_bytes(e));
 }
 
@@ -456,8 +457,8 @@ cudaError_t launch_reference_order_dup(const float* pos, int64_t n_pad_total, fl
   return cudaGetLastError();
 }
 
-cudaError_t launch_reference_order(int index, const ForceArgs& a, const float4* dup, int grid,
-                                   cudaStream_t stream) {
+cudaError_t launch_reference_order(int index, bool predicated, const ForceArgs& a,
+                                   const float4* dup, int grid, cudaStream_t stream) {
   const RoShapeEntry& e = kRoShapes[index];
   const cudaError_t err = ro_smem_opt_in(index);
   if (err != cudaSuccess) return err;
@@ -473,7 +474,7 @@ cudaError_t launch_reference_order(int index, const ForceArgs& a, const float4* 
   cfg.stream = stream;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, e.kernel, a, dup);
+  return cudaLaunchKernelEx(&cfg, e.kernel[predicated], a, dup);
 }
 
 }  // namespace nbg

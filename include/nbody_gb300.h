@@ -46,7 +46,10 @@ typedef enum nb_status {
 
 /* Kernel variant of the reference (sim_param.hpp:8-11).  PREDICATED reproduces
  * the reference as shipped: its pair term is multiplied by (j == i), so the
- * force is zero except where a pair term is not finite (simulator.cu:208-209). */
+ * force is zero except where a pair term is not finite (simulator.cu:208-209).  It
+ * runs the reference-order kernel's tiling with that pair term for equal masses,
+ * and one thread per particle for per-particle masses; the results are the
+ * reference kernel's, bit for bit. */
 typedef enum nb_calc_method { NB_BRANCH = 0, NB_PREDICATED = 1 } nb_calc_method;
 
 /* Per-particle force accumulator; the pair arithmetic is FP32 in every mode.
@@ -183,7 +186,8 @@ int nb_sim_advance_per_system(nb_sim* s, int32_t iterations);
  * first shared-memory tile of every CTA uncopied, so each CTA's bounded wait
  * (2 s) runs out; the launch writes no results, and the next
  * nb_sim_synchronize / nb_sim_get_state returns NB_ERR_DEVICE_TIMEOUT.  No
- * memory is faulted and nothing hangs; the simulation stays usable. */
+ * memory is faulted and nothing hangs; the simulation stays usable.  BRANCH
+ * method only (NB_ERR_STATE otherwise). */
 int nb_sim_inject_wait_timeout(nb_sim* s);
 /* Failure-detection test hook, host side only: the `nth` device allocation the
  * library makes from now on (1 = the next one, in any thread) fails with
@@ -271,7 +275,8 @@ int nb_sim_kernel_info(const nb_sim* s, nb_kernel_info* info);
 /* Time every kernel shape on this simulation's data (accelerations only, the
  * state is not advanced) and keep the fastest; `chosen` may be NULL.  With
  * NB_ACC_REFERENCE_ORDER it times that kernel's shapes (all give the same bits)
- * and reports -1 - shape; a no-op for NB_PREDICATED, whose kernel has one shape. */
+ * and reports -1 - shape; a no-op for NB_PREDICATED (it keeps its default shape,
+ * reported as -1 - shape). */
 int nb_sim_autotune(nb_sim* s, int32_t* chosen);
 
 /* Plan the work list of kernel shape `config_index` for systems of the given

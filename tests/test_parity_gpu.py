@@ -142,6 +142,27 @@ def test_predicated_matches_oracle_bitwise():
         assert np.array_equal(g, r)
 
 
+def _same_words(a, b):
+    return np.array_equal(np.asarray(a, np.float32).view(np.uint32),
+                          np.asarray(b, np.float32).view(np.uint32))
+
+
+@pytest.mark.parametrize("mass", ["random", "equal"])
+def test_predicated_both_kernels_match_oracle_bitwise(mass):
+    # Equal masses run the sequential-order kernel with the PREDICATED pair term;
+    # per-particle masses keep the one-thread-per-particle kernel.  Both give the
+    # oracle's words, here with a coincident pair (0 * rsqrt(...) of a finite term).
+    n = 3001
+    sim, pos, vel, m = make_sim(n, seed=43, method=nb.PREDICATED, mass=mass)
+    with sim:
+        sim.advance(2)
+        got = sim.get_state()
+    om, G = oracle_G(m)
+    ref = orc.run_fp32(pos, vel, om, G, 1e-3, 0.999, 1e-3, iters=2, method=orc.PREDICATED)
+    for g, r in zip(got, ref):
+        assert _same_words(g, r)
+
+
 def test_predicated_zero_softening_gives_nan_like_reference():
     n = 64
     sim, pos, vel, m = make_sim(n, seed=42, eps=0.0, method=nb.PREDICATED, mass="unit")
@@ -254,6 +275,26 @@ def test_accelerations_match_reference_kernel(n):
     # and the oracle against the reference kernel
     rms, mx = vec_errors(orc.accel_fp32(pos, None, 1.0, 1e-3), out[3:])
     assert rms <= ACC_RMS and mx <= ACC_MAX
+
+
+@needs_ref
+@pytest.mark.parametrize("n,eps", [(300000, 1e-3), (5000, 0.0)])
+def test_predicated_stream_k_matches_reference_kernel_bitwise(n, eps):
+    # At N = 300,000 the PREDICATED mode runs the sequential-order kernel with split
+    # i-tiles handed over between CTAs; eps = 0 turns every particle's sum to NaN
+    # through its own 0 * rsqrt(0) term, as in the reference.
+    pos, vel, _ = disk_case(n, seed=3 * n + 1)
+    ref, _ = orc.reference_run(pos, vel, 2.0, 1e-3, 0.999, eps, iters=2, method=nb.PREDICATED,
+                               gw_size=128)
+    with nb.Simulation(params(n, G=2.0, eps=eps, method=nb.PREDICATED), pos, vel, None) as sim:
+        info = sim.kernel_info()
+        sim.advance(2)
+        got = sim.get_state()
+    assert info["config_index"] <= -1
+    if n == 300000:
+        assert info["split_tiles"] > 0
+    for g, r in zip(got, ref):
+        assert _same_words(g, r)
 
 
 @needs_ref
