@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
     const uint32_t slot = issued % STAGES;
     // Failure-detection test: leave the first tile's barrier without arrival or
     // copy, so the consumers' bounded wait on it runs out.
-    if (!(a.skip_first_tile && issued == 0)) {
+    if (!(a.inject == kInjectSkipFirstTile && issued == 0)) {
       fence_proxy_async_smem();
       mbar_arrive_expect_tx(&full_bar[slot], static_cast<uint32_t>(count) * 16u);
       bulk_g2s(smem + slot * TILE_BYTES, a.pos + first * 4, static_cast<uint32_t>(count) * 16u,

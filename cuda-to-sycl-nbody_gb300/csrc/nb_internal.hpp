@@ -86,8 +86,14 @@ struct ForceArgs {
   float dt;
   float damping;
   int32_t mask_self;        // 1: exclude j == i explicitly (eps2^3 underflows)
-  int32_t skip_first_tile;  // failure-detection test: never copy each CTA's first j-tile
+  int32_t inject;           // failure-detection test hook (kInject*), 0 normally
 };
+
+// Failure-detection test hooks (ForceArgs::inject), one launch each; neither
+// faults anything, each makes a bounded device-side wait run out.
+constexpr int32_t kInjectSkipFirstTile = 1;     // no CTA copies its first j-tile
+constexpr int32_t kInjectWithholdHandOver = 2;  // sequential-order kernel: no CTA hands
+                                                // its running sums over
 
 // Host description of one kernel shape.
 struct KernelShape {

@@ -78,7 +78,7 @@ struct nb_sim {
   int32_t* err_d = nullptr;
   bool per_pair_mass = false;
   int32_t mask_self = 0;
-  int32_t inject_timeout = 0;  // one-shot failure-detection switch
+  int32_t inject = 0;  // one-shot failure-detection hook for the next force launch (kInject*)
 
   int cfg = 0;
   nbg::WorkListDev wl;

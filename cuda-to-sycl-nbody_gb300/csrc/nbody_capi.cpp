@@ -347,13 +347,13 @@ ForceArgs base_args(nb_sim* s) {
   a.dt = s->params.dt;
   a.damping = s->params.damping;
   a.mask_self = s->mask_self;
-  a.skip_first_tile = 0;
+  a.inject = 0;
   return a;
 }
 
 int launch_with(nb_sim* s, ForceArgs a, const WorkListDev& w) {
-  a.skip_first_tile = s->inject_timeout;
-  s->inject_timeout = 0;
+  a.inject = s->inject;
+  s->inject = 0;
   a.segs = w.segs;
   a.seg_begin = w.seg_begin;
   a.fix = w.fix;
@@ -1199,11 +1199,19 @@ int nb_sim_generate(nb_sim* s, int32_t kind, uint64_t seed) {
 }
 
 int nb_sim_inject_wait_timeout(nb_sim* s) {
+  return nb_sim_inject_failure(s, NB_INJECT_TILE_NEVER_COPIED);
+}
+
+int nb_sim_inject_failure(nb_sim* s, int32_t kind) {
   if (!s) return set_error(NB_ERR_INVALID_ARGUMENT, "sim is NULL");
   DeviceGuard dg_(s->device);
+  if (kind != NB_INJECT_TILE_NEVER_COPIED && kind != NB_INJECT_HAND_OVER_WITHHELD)
+    return set_error(NB_ERR_INVALID_ARGUMENT, "unknown failure kind");
   if (s->params.calc_method != NB_BRANCH)
-    return set_error(NB_ERR_STATE, "the wait-timeout hook covers the BRANCH kernels only");
-  s->inject_timeout = 1;
+    return set_error(NB_ERR_STATE, "the failure hooks cover the BRANCH kernels only");
+  if (kind == NB_INJECT_HAND_OVER_WITHHELD && !reference_order_mode(s))
+    return set_error(NB_ERR_STATE, "hand-overs exist in NB_ACC_REFERENCE_ORDER only");
+  s->inject = kind == NB_INJECT_TILE_NEVER_COPIED ? kInjectSkipFirstTile : kInjectWithholdHandOver;
   return NB_OK;
 }
 

@@ -246,7 +246,7 @@ extern "C" int nb_accelerations_noalloc(const float* pos_xyzm_device, uint64_t n
     const float e3 = dist_eps * dist_eps * dist_eps;
     a.mask_self = (e3 >= FLT_MIN) ? 0 : 1;
   }
-  a.skip_first_tile = 0;
+  a.inject = 0;
   NB_CUDA(launch_force(kNaConfig, false, true, a, grid, st));
   int32_t err = 0;
   NB_CUDA(cudaMemcpyAsync(&err, base + kOffErr, sizeof(err), cudaMemcpyDeviceToHost, st));

@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(THREADS, MINB) reference_order_kernel(
     const uint32_t slot = issued % kRoStages;
     // Failure-detection test: leave the first tile's barrier without arrival or
     // copy, so the consumers' bounded wait on it runs out.
-    if (!(a.skip_first_tile && issued == 0)) {
+    if (!(a.inject == kInjectSkipFirstTile && issued == 0)) {
       ro_fence_proxy_async();
       ro_arrive_expect_tx(&full_bar[slot], static_cast<uint32_t>(count) * 32u);
       ro_bulk_g2s(ring(slot), dup + 2 * first, static_cast<uint32_t>(count) * 32u,
@@ -368,7 +368,8 @@ __global__ void __launch_bounds__(THREADS, MINB) reference_order_kernel(
       }
       __threadfence();
       __syncthreads();
-      if (tid == 0) atomicAdd(&a.counters[sg.fix], 1);
+      // (Failure-detection test: withhold it, so the next part's bounded wait runs out.)
+      if (tid == 0 && a.inject != kInjectWithholdHandOver) atomicAdd(&a.counters[sg.fix], 1);
       continue;
     }
     if (split && tid == 0) a.counters[sg.fix] = 0;  // every part has run: reset for the next launch

@@ -35,6 +35,8 @@ ACC_COMPENSATED = 1
 ACC_REFERENCE_ORDER = 2
 BLOCK_POSITIONS = 1
 BLOCK_VELOCITIES = 2
+INJECT_TILE_NEVER_COPIED = 1
+INJECT_HAND_OVER_WITHHELD = 2
 IC_THIN_DISK = 1
 IC_PLUMMER = 2
 IC_TWO_DISKS = 3
@@ -108,6 +110,7 @@ SIGNATURES = {
     "nb_sim_advance_per_system": (C.c_int, [_P, C.c_int32]),
     "nb_sim_synchronize": (C.c_int, [_P]),
     "nb_sim_inject_wait_timeout": (C.c_int, [_P]),
+    "nb_sim_inject_failure": (C.c_int, [_P, C.c_int32]),
     "nb_sim_generate": (C.c_int, [_P, C.c_int32, C.c_uint64]),
     "nb_camera_matrices": (C.c_int, [C.c_float, C.c_float, C.c_float, _F, C.c_int32, C.c_int32,
                                      _F, _F]),
@@ -410,6 +413,10 @@ class Simulation:
     def inject_wait_timeout(self) -> None:
         """Failure-detection test hook: the next launch's bounded waits run out."""
         _check(lib.nb_sim_inject_wait_timeout(self._h))
+
+    def inject_failure(self, kind: int) -> None:
+        """Failure-detection test hook (INJECT_*) for the next force launch."""
+        _check(lib.nb_sim_inject_failure(self._h, kind))
 
     def time_iterations(self, iterations: int, per_system: int = 0) -> float:
         """Device milliseconds of `iterations` iterations (CUDA events).  per_system:

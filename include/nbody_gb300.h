@@ -187,8 +187,23 @@ int nb_sim_advance_per_system(nb_sim* s, int32_t iterations);
  * (2 s) runs out; the launch writes no results, and the next
  * nb_sim_synchronize / nb_sim_get_state returns NB_ERR_DEVICE_TIMEOUT.  No
  * memory is faulted and nothing hangs; the simulation stays usable.  BRANCH
- * method only (NB_ERR_STATE otherwise). */
+ * method only (NB_ERR_STATE otherwise).  Same as
+ * nb_sim_inject_failure(s, NB_INJECT_TILE_NEVER_COPIED). */
 int nb_sim_inject_wait_timeout(nb_sim* s);
+/* Failure-detection test hooks (one shot, the next force launch), each making one
+ * kind of bounded device-side wait run out without faulting anything:
+ *   NB_INJECT_TILE_NEVER_COPIED   as nb_sim_inject_wait_timeout;
+ *   NB_INJECT_HAND_OVER_WITHHELD  NB_ACC_REFERENCE_ORDER only: no CTA hands the
+ *                                 running sums of a split i-tile over, so the CTA
+ *                                 that continues it gives up after 2 s.
+ * The next nb_sim_synchronize / nb_sim_get_state returns NB_ERR_DEVICE_TIMEOUT and
+ * the simulation stays usable.  No reference counterpart (the reference exits on
+ * any CUDA error, simulator.cuh:22-31). */
+typedef enum nb_inject_kind {
+  NB_INJECT_TILE_NEVER_COPIED = 1,
+  NB_INJECT_HAND_OVER_WITHHELD = 2
+} nb_inject_kind;
+int nb_sim_inject_failure(nb_sim* s, int32_t kind);
 /* Failure-detection test hook, host side only: the `nth` device allocation the
  * library makes from now on (1 = the next one, in any thread) fails with
  * NB_ERR_OUT_OF_MEMORY without calling cudaMalloc; 0 disarms it.  Lets tests

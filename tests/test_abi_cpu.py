@@ -284,7 +284,8 @@ def test_null_handles_are_rejected_without_touching_the_device():
     L = nb.lib
     one = [(L.nb_sim_step, (h,)), (L.nb_sim_advance, (h, 1)),
            (L.nb_sim_advance_per_system, (h, 1)), (L.nb_sim_synchronize, (h,)),
-           (L.nb_sim_inject_wait_timeout, (h,)), (L.nb_sim_generate, (h, 1, 1)),
+           (L.nb_sim_inject_wait_timeout, (h,)), (L.nb_sim_inject_failure, (h, 1)),
+           (L.nb_sim_generate, (h, 1, 1)),
            (L.nb_sim_get_state, (h,) + (None,) * 6), (L.nb_sim_set_state, (h,) + (None,) * 7),
            (L.nb_sim_accelerations, (h, None, None, None)),
            (L.nb_sim_set_stream, (h, None)), (L.nb_sim_export_device, (h, None, None)),

@@ -32,6 +32,40 @@ def test_bounded_wait_timeout_is_reported_and_recoverable():
     assert max(float(np.max(np.abs(g - r))) for g, r in zip(got[:3], ref[:3])) <= 1e-4 * scale
 
 
+def test_withheld_hand_over_times_out_and_is_recoverable():
+    # NB_ACC_REFERENCE_ORDER at N = 150,000: 196 i-tiles of 768 on 152 CTAs, so split
+    # i-tiles are handed over between CTAs.  With the hand-overs withheld, each CTA
+    # that continues one gives up after its bounded wait (no fault, no hang).
+    n = 150000
+    pos, vel, m = disk_case(n, seed=79)
+    p = params(n, acc=nb.ACC_REFERENCE_ORDER)
+    with nb.Simulation(p, pos, vel, m) as ref:
+        ref.advance(2)
+        want = ref.get_state()
+    with nb.Simulation(p, pos, vel, m) as sim:
+        assert sim.kernel_info()["split_tiles"] > 0
+        sim.inject_failure(nb.INJECT_HAND_OVER_WITHHELD)
+        sim.advance(1)
+        with pytest.raises(nb.NbError) as e:
+            sim.synchronize()
+        assert e.value.status == nb.NB_ERR_DEVICE_TIMEOUT
+        sim.set_state(pos, vel)                      # usable again, same bits as before
+        sim.advance(2)
+        got = sim.get_state()
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
+
+
+def test_failure_hook_arguments():
+    pos, vel, m = disk_case(256, seed=80)
+    with nb.Simulation(params(256), pos, vel, m) as sim:
+        for kind, status in ((3, nb.NB_ERR_INVALID_ARGUMENT),
+                             (nb.INJECT_HAND_OVER_WITHHELD, nb.NB_ERR_STATE)):
+            with pytest.raises(nb.NbError) as e:
+                sim.inject_failure(kind)
+            assert e.value.status == status
+
+
 def test_errors_do_not_cross_the_abi_as_exceptions():
     n = 64
     pos, vel, m = disk_case(n, seed=78)
