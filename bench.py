@@ -491,7 +491,7 @@ def bench_render(sim, n) -> dict:
 
 
 def bench_ensemble(args) -> dict:
-    """Config 3: 4,096 Plummer systems, sizes log-uniform in [64, 8192]."""
+    """The ensemble workload: 4,096 Plummer systems, sizes log-uniform in [64, 8192]."""
     import torch
 
     import nbody_gb300 as nb
@@ -545,7 +545,7 @@ def bench_ensemble(args) -> dict:
 
 
 def bench_adjoint(args) -> dict:
-    """Config 4: N = 16,384 disk, T = 256 iterations, checkpoints every 16.  Forward
+    """The adjoint workload: N = 16,384 disk, T = 256 iterations, checkpoints every 16.  Forward
     and backward are both timed with CUDA events on the simulation's stream; the
     backward runs on device-resident gradients (nb_sim_adjoint_backward_device)."""
     import torch
@@ -590,7 +590,7 @@ def bench_adjoint(args) -> dict:
 
 # --------------------------------------------------------------------------- precision study
 def run_precision_study(args) -> dict:
-    """Config 2: N = 262,144 two-disk collision, plain vs compensated vs reference-order
+    """The precision study: N = 262,144 two-disk collision, plain vs compensated vs reference-order
     (the reference kernel's own summation, bit for bit) FP32 accumulation.
     FP64 energy and momenta (GPU) and the force error against FP64 accelerations on
     sampled rows every `every` steps.  Damping is 1 so that energy is conserved by the
@@ -654,19 +654,19 @@ def run_accuracy_study(args) -> dict:
 
     cases = []
     (x, y, z), (vx, vy, vz), m = nb.thin_disk(SEED, 25600, 1e-3)
-    cases.append(("config0_disk_25600", [x, y, z], [vx, vy, vz], m, None, 1e-3))
+    cases.append(("thin_disk_25600", [x, y, z], [vx, vy, vz], m, None, 1e-3))
     (x, y, z), (vx, vy, vz), m = nb.plummer(SEED, 1 << 20)
-    cases.append(("config1_plummer_1048576", [x, y, z], [vx, vy, vz], m, None, 1e-4))
+    cases.append(("plummer_1048576", [x, y, z], [vx, vy, vz], m, None, 1e-4))
     (x, y, z), (vx, vy, vz), m = nb.two_disks(SEED, 262144, 1e-3)
-    cases.append(("config2_two_disks_262144", [x, y, z], [vx, vy, vz], m, None, 1e-3))
+    cases.append(("two_disks_262144", [x, y, z], [vx, vy, vz], m, None, 1e-3))
     sizes = nb.ensemble_sizes(SEED, 4096, 64, 8192)
     parts = [nb.plummer(SEED + 1 + k, int(s_)) for k, s_ in enumerate(sizes)]
-    cases.append(("config3_ensemble_4096_systems",
+    cases.append(("ensemble_4096_systems",
                   [np.concatenate([q[0][c] for q in parts]) for c in range(3)],
                   [np.concatenate([q[1][c] for q in parts]) for c in range(3)],
                   np.concatenate([q[2] for q in parts]), sizes, 1e-3))
     (x, y, z), (vx, vy, vz), m = nb.thin_disk(SEED, 16384, 1e-3)
-    cases.append(("config4_disk_16384", [x, y, z], [vx, vy, vz], m, None, 1e-3))
+    cases.append(("adjoint_disk_16384", [x, y, z], [vx, vy, vz], m, None, 1e-3))
     out = {"study": "accuracy", "rows": 2048, "reference": "GPU FP64 all-pairs rows "
            "(nb_sim_fp64_accelerations), checked against the CPU FP64 oracle in the tests",
            "cases": {}}
@@ -689,7 +689,7 @@ def run_accuracy_study(args) -> dict:
 def run_sizes_study(args) -> dict:
     """ms per step of the tuned kernel (compensated, default shape), of the
     reference-order kernel (default shape) and of the PREDICATED compatibility kernel
-    from N = 2,048 to 1,048,576 (config-0 style thin disks, eps2 = 1e-3), CUDA events,
+    from N = 2,048 to 1,048,576 (thin disks, eps2 = 1e-3), CUDA events,
     median of repeated launches."""
     import nbody_gb300 as nb
 
@@ -786,8 +786,8 @@ def main() -> int:
                          "one replica per GPU")
     ap.add_argument("--study", choices=["precision", "accuracy", "ensemble", "sizes"],
                     default=None,
-                    help="run a study instead of the benchmark (precision: config 2 over time; "
-                         "accuracy: force error vs FP64 of every config, every accumulator; "
+                    help="run a study instead of the benchmark (precision: the two-disk collision over time; "
+                         "accuracy: force error vs FP64 of every workload, every accumulator; "
                          "ensemble: the 4,096-system ensemble leg alone, for profiling; "
                          "sizes: both kernels from N = 2,048 to 1M)")
     ap.add_argument("--study-steps", type=int, default=1000)

@@ -43,9 +43,9 @@ def cases():
     yield ("perf_args_n1280", [x, y, z], [vx, vy, vz],
            dict(G=2.0, dt=float(f32(0.001)), damping=float(f32(0.999)), eps=float(f32(1e-3)),
                 method=0, iters=5, gw=128))
-    # 3. config-0 style disk, m = 1/N folded into G (10 iterations)
+    # 3. thin disk (N = 2,048), m = 1/N folded into G (10 iterations)
     pos, vel, m = disk(2048, 2024)
-    yield ("config0_n2048", pos, vel,
+    yield ("thin_disk_n2048", pos, vel,
            dict(G=float(f32(1.0) * m[0]), dt=float(f32(1e-3)), damping=float(f32(0.999)),
                 eps=float(f32(1e-3)), method=0, iters=10, gw=64))
     # 4. force sums: damping 0, dt 1, G 1 makes v' the kernel's force accumulator

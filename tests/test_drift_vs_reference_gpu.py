@@ -1,5 +1,5 @@
 """Energy and momentum drift against the reference's own kernel: the same
-config-0-style disk (N = 25,600, m = 1/N, G = 1, eps2 = 1e-3, dt = 1e-3, damping 1
+thin disk (N = 25,600, m = 1/N, G = 1, eps2 = 1e-3, dt = 1e-3, damping 1
 so both are conserved) advanced 300 iterations by the reference kernel
 (src/simulator.cu:186-229, built unmodified for sm_103a) and by this library; the
 FP64 diagnostics of each final state.  The library's drift must be no worse."""

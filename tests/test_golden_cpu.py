@@ -27,7 +27,7 @@ def load(name):
 
 
 def test_golden_set_present():
-    assert {"config0_n2048", "force_sum_n1000", "perf_args_n1280", "predicated_n512",
+    assert {"thin_disk_n2048", "force_sum_n1000", "perf_args_n1280", "predicated_n512",
             "ragged_n333", "reference_default_n1024"} <= set(CASES)
     idx = json.loads((GOLDEN / "index.json").read_text())
     assert len(idx["cubin_sha256"]) == 64

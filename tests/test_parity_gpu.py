@@ -103,7 +103,7 @@ def test_ten_steps_match_oracle(acc, mass):
     assert dv <= POS_REL * vscale
 
 
-def test_config0_accelerations_against_fp64():
+def test_thin_disk_25600_accelerations_against_fp64():
     # N = 25,600 thin disk, eps2 = 1e-3, m = 1/N, G = 1 (the CPU-runnable case).
     n = 25600
     sim, pos, vel, m = make_sim(n, seed=2024)

@@ -36,7 +36,7 @@ def ro_params(n, **kw):
 
 
 def test_branch_golden_cases_present():
-    assert {"config0_n2048", "force_sum_n1000", "perf_args_n1280", "ragged_n333",
+    assert {"thin_disk_n2048", "force_sum_n1000", "perf_args_n1280", "ragged_n333",
             "reference_default_n1024"} <= set(BRANCH_CASES)
 
 
@@ -189,7 +189,7 @@ def test_random_cases_bitwise_equal_to_reference_kernel(seed):
 
 @needs_reference
 def test_thousand_steps_bitwise_equal_to_reference_kernel():
-    """1000 iterations of the config-0 disk (N = 25,600, unit masses with G = 1/N):
+    """1000 iterations of the 25,600-particle thin disk (N = 25,600, unit masses with G = 1/N):
     the trajectories are chaotic, so any single rounding difference would have
     grown into visible divergence; every word still matches."""
     n, iters = 25600, 1000
