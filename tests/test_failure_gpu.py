@@ -33,10 +33,10 @@ def test_bounded_wait_timeout_is_reported_and_recoverable():
 
 
 def test_withheld_hand_over_times_out_and_is_recoverable():
-    # NB_ACC_REFERENCE_ORDER at N = 150,000: 196 i-tiles of 768 on 152 CTAs, so split
+    # NB_ACC_REFERENCE_ORDER at N = 300,000: 196 i-tiles of 1536 on 152 CTAs, so split
     # i-tiles are handed over between CTAs.  With the hand-overs withheld, each CTA
     # that continues one gives up after its bounded wait (no fault, no hang).
-    n = 150000
+    n = 300000
     pos, vel, m = disk_case(n, seed=79)
     p = params(n, acc=nb.ACC_REFERENCE_ORDER)
     with nb.Simulation(p, pos, vel, m) as ref:

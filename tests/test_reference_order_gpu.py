@@ -229,7 +229,7 @@ def test_every_shape_and_autotune_stay_bitwise(n):
         got = sim.get_state()
     assert default <= -1
     if n == 25600:
-        assert default == -3          # 64 x 1: 200 i-tiles (384 x 2 would give 34)
+        assert default == -3          # 64 x 1: 200 i-tiles (384 x 2 would give 17)
     else:
-        assert default == -1          # 384 x 2: 391 (n = 300,000) or 1366 i-tiles
+        assert default == -1          # 384 x 2: 196 (n = 300,000) or 683 i-tiles
     assert same_bits(got, ref)
