@@ -138,3 +138,24 @@ def test_reference_order_is_the_reference_kernel_bit_for_bit(case, reference_sum
         st = sim.get_state()
     for g, r in zip(st, ref):
         assert np.array_equal(g, r), name
+
+
+def test_ensemble_workload_against_fp64_rows():
+    # The 4,096-system ensemble (sizes log-uniform in [64, 8192], about 6.6M particles,
+    # eps2 = 1e-3): FP32 accelerations of one persistent launch against FP64 rows
+    # spread over every system, for the default accumulator and the plain one.
+    sizes = nb.ensemble_sizes(SEED, 4096, 64, 8192)
+    parts = [nb.plummer(SEED + 1 + k, int(s)) for k, s in enumerate(sizes)]
+    pos = [np.concatenate([q[0][c] for q in parts]) for c in range(3)]
+    vel = [np.concatenate([q[1][c] for q in parts]) for c in range(3)]
+    m = np.concatenate([q[2] for q in parts])
+    n = pos[0].size
+    rows = np.linspace(0, n - 1, 2048).astype(np.int64)
+    eps = float(np.float32(1e-3))
+    for acc, bound in ((nb.ACC_COMPENSATED, ACC_RMS), (nb.ACC_PLAIN, ACC_RMS)):
+        with nb.Simulation(params(n, eps=eps, acc=acc), pos, vel, m, sizes=sizes) as sim:
+            got = sim.accelerations()
+            f64 = sim.fp64_accelerations(rows.astype(np.uint64))
+        rms, mx = vec_errors(_rows(got, rows), f64)
+        print(f"ensemble_4096_systems: accumulator {acc} vs FP64 rel RMS {rms:.3g}, max {mx:.3g}")
+        assert rms <= bound and mx <= ACC_MAX, (acc, rms, mx)
