@@ -233,3 +233,31 @@ def test_every_shape_and_autotune_stay_bitwise(n):
     else:
         assert default == -1          # 384 x 2: 196 (n = 300,000) or 683 i-tiles
     assert same_bits(got, ref)
+
+
+@needs_reference
+def test_shape_selection_by_index_stays_bitwise():
+    # nb_sim_set_kernel_config selects the reference-order kernel's shapes by index in
+    # this mode (reported back as -1 - index); every shape gives the reference's bits.
+    n = 40000
+    pos, vel, _ = disk_case(n, seed=37)
+    G = float(np.float32(1.0 / n))
+    ref, _ = orc.reference_run(pos, vel, G, 1e-3, 0.999, 1e-3, iters=2, method=orc.BRANCH)
+    p = nb.SimParam(numParticles=n, G=G, dt=1e-3, damping=0.999, distEps=1e-3,
+                    calcMethod=nb.BRANCH, accumulator=nb.ACC_REFERENCE_ORDER)
+    with nb.Simulation(p, pos, vel, None) as sim:
+        shapes = 0
+        while True:
+            try:
+                sim.set_kernel_config(shapes)
+            except nb.NbError as e:
+                assert e.status == nb.NB_ERR_INVALID_ARGUMENT
+                break
+            assert sim.kernel_info()["config_index"] == -1 - shapes
+            sim.set_state(pos, vel)
+            sim.advance(2)
+            assert same_bits(sim.get_state(), ref), shapes
+            shapes += 1
+        assert shapes == 3
+        sim.set_kernel_config(-1)                     # back to the default
+        assert sim.kernel_info()["config_index"] <= -1
