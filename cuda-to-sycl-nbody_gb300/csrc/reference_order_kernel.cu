@@ -400,7 +400,10 @@ struct RoShapeEntry {
 // launch): 384 x 2 with 1024-particle j-tiles 69.8 % (12 warps, one CTA per SM);
 // 384 x 2 x 256 69.0 %; 512 x 2 67.9 % (16 warps, 128 registers); 256 x 2 66.5 %
 // (8 warps); 128 x 4 65.9 %; 128 x 2 64.2 %; 448 x 2 and 320 x 2 (warps not a
-// multiple of the SM's four schedulers) 59 %; 64 x 1 53.4 %.  The small shapes
+// multiple of the SM's four schedulers) 59 %; 64 x 1 53.4 %; 384 x 2 x 2048 69.9 %,
+// 256 x 4 69.4 %, 384 x 3 69.2 %, 256 x 3 68.3 %, 384 x 2 with 2 j steps per unrolled
+// block 65.5 % (at N = 262,144 the three-and-four-pair shapes fall to 51-68 %: fewer,
+// larger i-tiles balance worse).  The small shapes
 // serve systems too small to fill the GPU with the large i-tiles.
 const RoShapeEntry kRoShapes[] = {
     RO_SHAPE(384, 2, 1024, 4, 1),
