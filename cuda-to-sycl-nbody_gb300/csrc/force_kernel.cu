@@ -28,13 +28,14 @@ int num_force_configs() { return kNumForceShapesA + kNumForceShapesB + kNumForce
 
 KernelShape force_config_shape(int index) { return entry(index).shape; }
 
-cudaError_t launch_force(int index, bool compensated, bool per_pair_mass, const ForceArgs& a,
-                         int grid, cudaStream_t stream) {
-  return entry(index).launch[compensated][per_pair_mass](a, grid, stream);
+cudaError_t launch_force(int index, bool compensated, bool per_pair_mass, bool live,
+                         const ForceArgs& a, int grid, cudaStream_t stream) {
+  return entry(index).launch[live][compensated][per_pair_mass](a, grid, stream);
 }
 
-cudaError_t force_blocks_per_sm(int index, bool compensated, bool per_pair_mass, int* blocks) {
-  return entry(index).occ[compensated][per_pair_mass](blocks);
+cudaError_t force_blocks_per_sm(int index, bool compensated, bool per_pair_mass, bool live,
+                                int* blocks) {
+  return entry(index).occ[live][compensated][per_pair_mass](blocks);
 }
 
 }  // namespace nbg

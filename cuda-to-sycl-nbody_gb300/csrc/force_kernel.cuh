@@ -49,11 +49,11 @@ using LaunchFn = cudaError_t (*)(const ForceArgs&, int, cudaStream_t);
 using OccFn = cudaError_t (*)(int*);
 
 // One compiled kernel shape: launchers and occupancy queries indexed by
-// [compensated][per_pair_mass].
+// [live_slots][compensated][per_pair_mass].
 struct ConfigEntry {
   KernelShape shape;
-  LaunchFn launch[2][2];
-  OccFn occ[2][2];
+  LaunchFn launch[2][2][2];
+  OccFn occ[2][2][2];
 };
 
 namespace {
@@ -147,9 +147,10 @@ __device__ __forceinline__ void kahan_finish(float2 s, float2 c, float& hi, floa
 }
 
 // Pair loop over `npairs` j-pairs of one shared-memory tile (npairs % 8 == 0), U
-// j-pairs per unrolled step.
+// j-pairs per unrolled step, for the first RL of the thread's R i-particles (the
+// others are past the end of the system and keep their zero sums).
 // kMask: zero the term of j == i (tiles overlapping the i-tile when eps2^3 underflows).
-template <int R, int U, bool kMass, bool kMask>
+template <int RL, int R, int U, bool kMass, bool kMask>
 __device__ __forceinline__ void tile_pairs(const float4* __restrict__ tile, int npairs, float2 e2,
                                            const float2 (&nx)[R], const float2 (&ny)[R],
                                            const float2 (&nz)[R], float2 (&ax)[R],
@@ -165,7 +166,7 @@ __device__ __forceinline__ void tile_pairs(const float4* __restrict__ tile, int 
       const float2 yy = make_float2(A.z, A.w);
       const float2 zz = make_float2(B.x, B.y);
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
+      for (int r = 0; r < RL; ++r) {
         const float2 dx = __fadd2_rn(xx, nx[r]);
         const float2 dy = __fadd2_rn(yy, ny[r]);
         const float2 dz = __fadd2_rn(zz, nz[r]);
@@ -189,11 +190,51 @@ __device__ __forceinline__ void tile_pairs(const float4* __restrict__ tile, int 
   }
 }
 
+// tile_pairs over the live register slots: `live` is live_slots() of the i-tile, one
+// of 1-4 or R, and only those loop variants are compiled.  Only the kernels built
+// with kLive carry these loops: their presence changes how ptxas allocates the full
+// loop (236 -> 240 registers for 256 x 4 x 2048, compensated, and 78.5 -> 75.2 % of
+// peak at N = 1M), so work lists whose i-tiles are all full keep the kernel without.
+template <int R, int U, bool kMass>
+__device__ __forceinline__ void tile_pairs_live(int live, const float4* __restrict__ tile,
+                                                int npairs, float2 e2, const float2 (&nx)[R],
+                                                const float2 (&ny)[R], const float2 (&nz)[R],
+                                                float2 (&ax)[R], float2 (&ay)[R], float2 (&az)[R],
+                                                int64_t j_first, const int64_t (&gi)[R]) {
+  if constexpr (R > 1) {
+    if (live == 1) {
+      tile_pairs<1, R, U, kMass, false>(tile, npairs, e2, nx, ny, nz, ax, ay, az, j_first, gi);
+      return;
+    }
+  }
+  if constexpr (R > 2) {
+    if (live == 2) {
+      tile_pairs<2, R, U, kMass, false>(tile, npairs, e2, nx, ny, nz, ax, ay, az, j_first, gi);
+      return;
+    }
+  }
+  if constexpr (R > 3) {
+    if (live == 3) {
+      tile_pairs<3, R, U, kMass, false>(tile, npairs, e2, nx, ny, nz, ax, ay, az, j_first, gi);
+      return;
+    }
+  }
+  if constexpr (R > 4) {
+    if (live == 4) {
+      tile_pairs<4, R, U, kMass, false>(tile, npairs, e2, nx, ny, nz, ax, ay, az, j_first, gi);
+      return;
+    }
+  }
+  tile_pairs<R, R, U, kMass, false>(tile, npairs, e2, nx, ny, nz, ax, ay, az, j_first, gi);
+}
+
 // __launch_bounds__(THREADS, 1): one resident CTA per SM is enough, so ptxas may use up
 // to 255 registers per thread for the R i-particles and the unrolled pair loop (with
 // the thread bound alone it caps 256-thread shapes at 128 registers, measured 17 %
 // slower).
-template <int THREADS, int R, int BJ, int STAGES, int U, bool kComp, bool kMass>
+// kLive: skip the register slots past the end of a system in its last i-tile
+// (tile_pairs_live); the work list must then be planned with live-slot weights.
+template <int THREADS, int R, int BJ, int STAGES, int U, bool kComp, bool kMass, bool kLive>
 __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
   constexpr int BI = THREADS * R;
   constexpr int TILE_BYTES = BJ * 16;
@@ -257,6 +298,7 @@ __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
     const SystemDesc sd = a.sys[sg.sys];
     const int ibase = sd.shard_first + sg.itile * BI;
     const int iend = shard_end(sd);
+    const int live = kLive ? live_slots(iend - ibase, THREADS, R) : R;  // slots to run
 
     float2 nx[R], ny[R], nz[R], ax[R], ay[R], az[R];
     float2 sx[R], sy[R], sz[R], cx[R], cy[R], cz[R];  // compensated running sums
@@ -285,9 +327,13 @@ __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
       const int64_t j_first = sd.offset + static_cast<int64_t>(jt) * BJ;
       const bool diag = a.mask_self && (jt * BJ < ibase + BI) && (ibase < jt * BJ + count);
       if (diag) {
-        tile_pairs<R, U, kMass, true>(tile, count >> 1, e2, nx, ny, nz, ax, ay, az, j_first, gi);
+        tile_pairs<R, R, U, kMass, true>(tile, count >> 1, e2, nx, ny, nz, ax, ay, az, j_first, gi);
+      } else if constexpr (kLive) {
+        tile_pairs_live<R, U, kMass>(live, tile, count >> 1, e2, nx, ny, nz, ax, ay, az, j_first,
+                                     gi);
       } else {
-        tile_pairs<R, U, kMass, false>(tile, count >> 1, e2, nx, ny, nz, ax, ay, az, j_first, gi);
+        tile_pairs<R, R, U, kMass, false>(tile, count >> 1, e2, nx, ny, nz, ax, ay, az, j_first,
+                                          gi);
       }
       if (kComp) {
 #pragma unroll
@@ -405,7 +451,7 @@ __global__ void __launch_bounds__(THREADS, 1) force_kernel(const ForceArgs a) {
 // (with the kernel's static shared memory the 48 KB default is exceeded at exactly
 // 48 KB). The attribute belongs to the kernel's instance on the current device, so
 // the opt-in is made once per device ordinal (ordinals >= 64 opt in on every call).
-template <int T, int R, int BJ, int S, int U, bool C, bool M>
+template <int T, int R, int BJ, int S, int U, bool C, bool M, bool L>
 cudaError_t smem_opt_in() {
   constexpr int smem = S * BJ * 16;
   if (smem < 48 * 1024) return cudaSuccess;
@@ -415,39 +461,45 @@ cudaError_t smem_opt_in() {
   if (e != cudaSuccess) return e;
   const uint64_t bit = dev >= 0 && dev < 64 ? uint64_t{1} << dev : 0;
   if (bit != 0 && (opted.load(std::memory_order_acquire) & bit) != 0) return cudaSuccess;
-  e = cudaFuncSetAttribute(force_kernel<T, R, BJ, S, U, C, M>,
+  e = cudaFuncSetAttribute(force_kernel<T, R, BJ, S, U, C, M, L>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e == cudaSuccess && bit != 0) opted.fetch_or(bit, std::memory_order_release);
   return e;
 }
 
-template <int T, int R, int BJ, int S, int U, bool C, bool M>
+template <int T, int R, int BJ, int S, int U, bool C, bool M, bool L>
 cudaError_t launch_one(const ForceArgs& a, int grid, cudaStream_t st) {
   constexpr int smem = S * BJ * 16;
-  const cudaError_t e = smem_opt_in<T, R, BJ, S, U, C, M>();
+  const cudaError_t e = smem_opt_in<T, R, BJ, S, U, C, M, L>();
   if (e != cudaSuccess) return e;
-  force_kernel<T, R, BJ, S, U, C, M><<<grid, T, smem, st>>>(a);
+  force_kernel<T, R, BJ, S, U, C, M, L><<<grid, T, smem, st>>>(a);
   return cudaGetLastError();
 }
 
-template <int T, int R, int BJ, int S, int U, bool C, bool M>
+template <int T, int R, int BJ, int S, int U, bool C, bool M, bool L>
 cudaError_t occ_one(int* blocks) {
   constexpr int smem = S * BJ * 16;
-  const cudaError_t e = smem_opt_in<T, R, BJ, S, U, C, M>();
+  const cudaError_t e = smem_opt_in<T, R, BJ, S, U, C, M, L>();
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, force_kernel<T, R, BJ, S, U, C, M>,
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, force_kernel<T, R, BJ, S, U, C, M, L>,
                                                        T, smem);
 }
 
 }  // namespace
 
-#define NBG_CONFIG(T, R, BJ, S, U)                                                          \
-  ConfigEntry {                                                                            \
-    KernelShape{T, R, BJ, S},                                                              \
-        {{launch_one<T, R, BJ, S, U, false, false>, launch_one<T, R, BJ, S, U, false, true>}, \
-         {launch_one<T, R, BJ, S, U, true, false>, launch_one<T, R, BJ, S, U, true, true>}},  \
-        {{occ_one<T, R, BJ, S, U, false, false>, occ_one<T, R, BJ, S, U, false, true>},       \
-         {occ_one<T, R, BJ, S, U, true, false>, occ_one<T, R, BJ, S, U, true, true>}},        \
+// One shape's launchers (NBG_LAUNCH_L) and occupancy queries (NBG_OCC_L) for one
+// value of kLive, as [compensated][per_pair_mass].
+#define NBG_LAUNCH_L(T, R, BJ, S, U, L)                                                       \
+  {{launch_one<T, R, BJ, S, U, false, false, L>, launch_one<T, R, BJ, S, U, false, true, L>}, \
+   {launch_one<T, R, BJ, S, U, true, false, L>, launch_one<T, R, BJ, S, U, true, true, L>}}
+#define NBG_OCC_L(T, R, BJ, S, U, L)                                                    \
+  {{occ_one<T, R, BJ, S, U, false, false, L>, occ_one<T, R, BJ, S, U, false, true, L>}, \
+   {occ_one<T, R, BJ, S, U, true, false, L>, occ_one<T, R, BJ, S, U, true, true, L>}}
+#define NBG_CONFIG(T, R, BJ, S, U)                                                  \
+  ConfigEntry {                                                                    \
+    KernelShape{T, R, BJ, S},                                                      \
+        {NBG_LAUNCH_L(T, R, BJ, S, U, false), NBG_LAUNCH_L(T, R, BJ, S, U, true)}, \
+        {NBG_OCC_L(T, R, BJ, S, U, false), NBG_OCC_L(T, R, BJ, S, U, true)},       \
   }
 
 }  // namespace nbg

@@ -52,6 +52,15 @@ __host__ __device__ inline int32_t shard_end(const SystemDesc& d) {
   return d.shard_count ? d.shard_first + d.shard_count : d.n;
 }
 
+// Register slots of a force-kernel thread (r i-particles at stride `threads`) that
+// hold a particle in an i-tile with `rows` particles to integrate: ceil(rows /
+// threads), capped at r, and raised to r when above 4 (the kernel has loop variants
+// for 1-4 slots and for all r).  The work-list planner charges an i-tile by it.
+__host__ __device__ inline int32_t live_slots(int32_t rows, int32_t threads, int32_t r) {
+  const int32_t live = rows <= threads ? 1 : (rows + threads - 1) / threads;
+  return live >= r ? r : (live <= 4 ? live : r);
+}
+
 // One entry of a CTA's work list: i-tile `itile` of system `sys` against j-tiles
 // [jt0, jt1).  `fix` >= 0 when the i-tile's j-range is split over several CTAs:
 // this entry is part `part` of fixup record `fix`.

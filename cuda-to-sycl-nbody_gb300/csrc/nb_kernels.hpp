@@ -11,10 +11,13 @@ namespace nbg {
 int num_force_configs();
 KernelShape force_config_shape(int index);
 // Launch the tuned force kernel of shape `index`.  `compensated` selects the Kahan
-// accumulator, `per_pair_mass` multiplies each pair term by m_j.
-cudaError_t launch_force(int index, bool compensated, bool per_pair_mass, const ForceArgs& a,
-                         int grid, cudaStream_t stream);
-cudaError_t force_blocks_per_sm(int index, bool compensated, bool per_pair_mass, int* blocks);
+// accumulator, `per_pair_mass` multiplies each pair term by m_j, `live` the variant
+// that skips the register slots past the end of a system (its work list is planned
+// with live-slot weights, live_slots_pay in worklist.hpp).
+cudaError_t launch_force(int index, bool compensated, bool per_pair_mass, bool live,
+                         const ForceArgs& a, int grid, cudaStream_t stream);
+cudaError_t force_blocks_per_sm(int index, bool compensated, bool per_pair_mass, bool live,
+                                int* blocks);
 
 // ---- compatibility kernel (aux_kernels.cu) ------------------------------------------
 // The reference's PREDICATED variant as shipped, one thread per i-particle over one

@@ -21,6 +21,7 @@ namespace nbg {
 // cfg < 0: reference-order shape -1 - cfg.
 struct WorkListDev {
   int32_t cfg = -1;
+  bool live = false;  // the force kernel's live-slot variant (planned with its weights)
   int32_t grid = 0;
   int32_t nseg = 0;
   int32_t nfix = 0;

@@ -204,11 +204,11 @@ static int ensure_scratch(nb_sim* s, const WorkListDev& w) {
   return NB_OK;
 }
 
-static int max_grid_for(nb_sim* s, int cfg) {
+static int max_grid_for(nb_sim* s, int cfg, bool live = false) {
   int blocks = 0;
   const bool comp = s->params.accumulator == NB_ACC_COMPENSATED;
   const cudaError_t e =
-      cfg >= 0 ? force_blocks_per_sm(cfg, comp, s->per_pair_mass, &blocks)
+      cfg >= 0 ? force_blocks_per_sm(cfg, comp, s->per_pair_mass, live, &blocks)
                : reference_order_blocks_per_sm(-1 - cfg, s->params.calc_method == NB_PREDICATED,
                                                &blocks);
   if (e != cudaSuccess || blocks < 1) blocks = 1;
@@ -252,13 +252,24 @@ static int upload_worklist(nb_sim* s, const WorkListHost& h, int cfg, WorkListDe
   return NB_OK;
 }
 
+// Plan systems [first, first + count) for tuned-kernel config `cfg` on at most
+// `grid` CTAs (0: the occupancy limit), with the live-slot variant where it pays.
+static int plan_tuned(nb_sim* s, int cfg, int32_t first, int32_t count, int grid,
+                      WorkListDev* out) {
+  const KernelShape sh = force_config_shape(cfg);
+  const bool live = live_slots_pay(s->sys_h.data(), first, count, sh.threads, sh.r);
+  if (grid <= 0) grid = max_grid_for(s, cfg, live);
+  const WorkListHost h = plan_worklist(s->sys_h.data(), first, count, sh.bi(), sh.bj, grid,
+                                       live ? sh.threads : 0, sh.r);
+  NB_TRY(upload_worklist(s, h, cfg, out));
+  out->live = live;
+  return NB_OK;
+}
+
 // (Re)build the all-systems work list for kernel config `cfg`.
 static int build_main_worklist(nb_sim* s, int cfg) {
-  const KernelShape sh = force_config_shape(cfg);
-  const WorkListHost h = plan_worklist(s->sys_h.data(), 0, static_cast<int32_t>(s->sys_h.size()),
-                                       sh.bi(), sh.bj, max_grid_for(s, cfg));
   WorkListDev w;
-  NB_TRY(upload_worklist(s, h, cfg, &w));
+  NB_TRY(plan_tuned(s, cfg, 0, static_cast<int32_t>(s->sys_h.size()), 0, &w));
   drop_graphs(s);
   free_worklist(s->wl);
   s->wl = w;
@@ -315,11 +326,15 @@ static int build_per_system_worklists(nb_sim* s, int policy) {
     int cfg = sim_cfg;
     if (policy == kPerSystemOwnShape)
       cfg = ro ? -1 - default_reference_order_for(s, k, 1) : default_config_for(s, k, 1);
-    const KernelShape sh = shape_of(cfg);
-    const int grid = cfg >= 0 ? max_grid_for(s, cfg) : reference_order_grid(s, -1 - cfg, k, 1);
-    const WorkListHost h = plan_worklist(s->sys_h.data(), k, 1, sh.bi(), sh.bj, grid);
     WorkListDev w;
-    NB_TRY(upload_worklist(s, h, cfg, &w));
+    if (cfg >= 0) {
+      NB_TRY(plan_tuned(s, cfg, k, 1, 0, &w));
+    } else {
+      const KernelShape sh = shape_of(cfg);
+      const WorkListHost h = plan_worklist(s->sys_h.data(), k, 1, sh.bi(), sh.bj,
+                                           reference_order_grid(s, -1 - cfg, k, 1));
+      NB_TRY(upload_worklist(s, h, cfg, &w));
+    }
     s->wl_sys.push_back(w);
   }
   s->wl_sys_policy = policy;
@@ -363,8 +378,8 @@ int launch_with(nb_sim* s, ForceArgs a, const WorkListDev& w) {
                                    s->ro_dup_d, w.grid, s->stream));
     return NB_OK;
   }
-  NB_CUDA(launch_force(w.cfg, s->params.accumulator == NB_ACC_COMPENSATED, s->per_pair_mass, a,
-                       w.grid, s->stream));
+  NB_CUDA(launch_force(w.cfg, s->params.accumulator == NB_ACC_COMPENSATED, s->per_pair_mass,
+                       w.live, a, w.grid, s->stream));
   return NB_OK;
 }
 
@@ -919,9 +934,9 @@ int nb_sim_export_device(nb_sim* s, float* pos_xyzm_device, float* vel_xyzw_devi
 int nb_num_kernel_configs(void) { return num_force_configs(); }
 
 int nb_kernel_config_info(int32_t index, nb_kernel_info* info) {
-  if (!info || index < 0 || index >= num_force_configs())
+  if (!info || index < -reference_order_num_shapes() || index >= num_force_configs())
     return set_error(NB_ERR_INVALID_ARGUMENT, "bad config index");
-  const KernelShape sh = force_config_shape(index);
+  const KernelShape sh = index >= 0 ? force_config_shape(index) : reference_order_shape(-1 - index);
   *info = nb_kernel_info{index, sh.threads, sh.r, sh.bj, sh.stages, 0, 0, 0};
   return NB_OK;
 }
@@ -1035,7 +1050,7 @@ int nb_plan_work(uint32_t num_systems, const uint32_t* sizes, int32_t config_ind
                  int32_t* num_partial_slots) {
   static_assert(sizeof(nb_segment) == sizeof(Segment), "nb_segment mirrors Segment");
   if (num_systems == 0 || !sizes) return set_error(NB_ERR_INVALID_ARGUMENT, "no systems");
-  if (config_index < 0 || config_index >= num_force_configs())
+  if (config_index < -reference_order_num_shapes() || config_index >= num_force_configs())
     return set_error(NB_ERR_INVALID_ARGUMENT, "bad config index");
   if (max_grid < 1) return set_error(NB_ERR_INVALID_ARGUMENT, "max_grid must be >= 1");
   std::vector<SystemDesc> sys(num_systems);
@@ -1048,9 +1063,14 @@ int nb_plan_work(uint32_t num_systems, const uint32_t* sizes, int32_t config_ind
     sys[k].npad = static_cast<int32_t>((sizes[k] + kPadQuantum - 1) / kPadQuantum * kPadQuantum);
     off += sys[k].npad;
   }
-  const KernelShape sh = force_config_shape(config_index);
-  const WorkListHost h =
-      plan_worklist(sys.data(), 0, static_cast<int32_t>(num_systems), sh.bi(), sh.bj, max_grid);
+  const bool tuned = config_index >= 0;
+  const KernelShape sh =
+      tuned ? force_config_shape(config_index) : reference_order_shape(-1 - config_index);
+  // The rule of every launch: the tuned kernel's live-slot variant where it pays.
+  const bool live = tuned && live_slots_pay(sys.data(), 0, static_cast<int32_t>(num_systems),
+                                            sh.threads, sh.r);
+  const WorkListHost h = plan_worklist(sys.data(), 0, static_cast<int32_t>(num_systems), sh.bi(),
+                                       sh.bj, max_grid, live ? sh.threads : 0, sh.r);
   if (grid) *grid = h.grid;
   if (num_segments) *num_segments = static_cast<int32_t>(h.segs.size());
   if (num_fixups) *num_fixups = static_cast<int32_t>(h.fix.size());

@@ -137,7 +137,7 @@ int na_setup(int dev, DeviceSetup* out) {
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(no-allocation scratch)");
     int blocks = 0;
-    NB_CUDA(force_blocks_per_sm(kNaConfig, false, true, &blocks));
+    NB_CUDA(force_blocks_per_sm(kNaConfig, false, true, false, &blocks));
     const KernelShape sh = force_config_shape(kNaConfig);
     if (sh.bi() != kNaBI || sh.bj != kNaBJ)
       return set_error(NB_ERR_STATE, "no-allocation kernel shape mismatch");
@@ -151,7 +151,8 @@ int na_setup(int dev, DeviceSetup* out) {
 }
 
 // The force kernel's stream-K plan (plan_work_into, the rule of every other
-// launch) for one system, written into the fixed host tables.  The bounds above
+// launch) for one system, written into the fixed host tables.  The kernel runs
+// every register slot here (no live-slot variant), so the plan is unweighted.  The bounds above
 // make it fit for every n <= kNaMaxParticles and grid <= kNaMaxGrid; false if not.
 bool na_plan(int32_t n, int32_t npad, int32_t grid_max, int32_t* grid, int32_t* nseg,
              int32_t* nfix, int32_t* nslots) {
@@ -247,7 +248,7 @@ extern "C" int nb_accelerations_noalloc(const float* pos_xyzm_device, uint64_t n
     a.mask_self = (e3 >= FLT_MIN) ? 0 : 1;
   }
   a.inject = 0;
-  NB_CUDA(launch_force(kNaConfig, false, true, a, grid, st));
+  NB_CUDA(launch_force(kNaConfig, false, true, false, a, grid, st));
   int32_t err = 0;
   NB_CUDA(cudaMemcpyAsync(&err, base + kOffErr, sizeof(err), cudaMemcpyDeviceToHost, st));
   NB_CUDA(cudaStreamSynchronize(st));

@@ -30,10 +30,11 @@ struct VectorTables {
 }  // namespace
 
 WorkListHost plan_worklist(const SystemDesc* sys, int32_t first, int32_t count, int32_t bi,
-                           int32_t bj, int32_t max_grid) {
+                           int32_t bj, int32_t max_grid, int32_t threads, int32_t r) {
   WorkListHost wl;
   VectorTables out{wl};
-  plan_work_into(sys, first, count, bi, bj, max_grid, out, &wl.slots, &wl.split_tiles);
+  plan_work_into(sys, first, count, bi, bj, max_grid, out, &wl.slots, &wl.split_tiles, threads,
+                 r);
   return wl;
 }
 

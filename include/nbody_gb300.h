@@ -277,9 +277,11 @@ int nb_sim_load_state_block(nb_sim* s, uint64_t first, uint64_t count, int32_t w
                             const void* src_device);
 
 /* ---- kernel selection ---------------------------------------------------------- */
-/* The compiled shapes of the tuned kernel.  No reference counterpart: the
- * reference launches ceil(N / gwSize) blocks of gwSize threads (simulator.cu:49-50),
- * and gwSize is only reported here (nb_sim_gw_size). */
+/* The compiled shapes of the tuned kernel (index 0 .. nb_num_kernel_configs() - 1);
+ * nb_kernel_config_info and nb_plan_work also take -1 - k for shape k of the
+ * reference-order kernel.  No reference counterpart: the reference launches
+ * ceil(N / gwSize) blocks of gwSize threads (simulator.cu:49-50), and gwSize is only
+ * reported here (nb_sim_gw_size). */
 int nb_num_kernel_configs(void);
 int nb_kernel_config_info(int32_t index, nb_kernel_info* info);
 /* Select a kernel shape by index (-1 = the built-in default for this size).  With
@@ -297,7 +299,10 @@ int nb_sim_autotune(nb_sim* s, int32_t* chosen);
 /* Plan the work list of kernel shape `config_index` for systems of the given
  * sizes on at most `max_grid` CTAs (host only; needs no GPU).  Every
  * (system, i-tile, j-tile) block is assigned to exactly one CTA and each CTA
- * gets the same number of pair interactions to within one j-tile.  `segments`
+ * gets the same work to within one block.  A block of the tuned kernel costs its
+ * j-tile length times the register slots it runs (the i-particles per thread, fewer
+ * only in a system's last, partly filled i-tile); a block of the reference-order
+ * kernel costs its j-tile length.  `segments`
  * (capacity max_segments) and `seg_begin` (capacity max_grid + 1) may be NULL to
  * query the counts only.  No reference counterpart (the reference launches one
  * thread per particle, simulator.cu:49-50). */

@@ -201,12 +201,25 @@ def test_reference_disk_matches_reference_generator():
 
 
 # ----------------------------------------------------------------- work-list planner
+def _live_slots(rows, threads, r):
+    # Register slots the tuned kernel runs for an i-tile with `rows` particles
+    # (live_slots in csrc/nb_internal.hpp): ceil(rows / threads), capped at r, raised
+    # to r when above 4.
+    live = max(1, -(-rows // threads))
+    return r if live >= r else (live if live <= 4 else r)
+
+
 @pytest.mark.parametrize("sizes,cfg,grid", [
     ([1048576], 0, 304), ([25600], 0, 456), ([1], 0, 304), ([17], 3, 8), ([5000], 4, 7),
-    ([64, 100, 8192, 3, 700], 3, 304), ([1000] * 50, 4, 152)])
+    ([64, 100, 8192, 3, 700], 3, 304), ([1000] * 50, 4, 152), ([100, 3000, 70, 9000], 2, 40),
+    ([100, 300, 70, 2000], 1, 40), ("ensemble", 9, 152),
+    ([64, 100, 8192, 3, 700], -1, 60), ([1048576], -1, 152), ([25600], -3, 152)])
 def test_plan_work_covers_every_tile_once(sizes, cfg, grid):
+    if sizes == "ensemble":  # 300 systems of the ensemble workload's size distribution
+        sizes = [int(n) for n in nb.ensemble_sizes(20261203, 300, 64, 8192)]
     info = nb.kernel_config_info(cfg)
-    bi = info["threads_per_block"] * info["particles_per_thread"]
+    threads, r = info["threads_per_block"], info["particles_per_thread"]
+    bi = threads * r
     bj = info["j_tile"]
     g, segs, begin, nfix, slots = nb.plan_work(sizes, cfg, grid)
     assert 1 <= g <= grid
@@ -214,6 +227,16 @@ def test_plan_work_covers_every_tile_once(sizes, cfg, grid):
     covered = {}
     cost = np.zeros(g, dtype=np.int64)
     npad = [(n + 15) // 16 * 16 for n in sizes]
+    # The tuned kernel's live-slot variant, and its weights, where it saves >= 1 % of
+    # the slot work (live_slots_pay in csrc/worklist.hpp); the reference-order kernel
+    # (cfg < 0) runs every slot.
+    def live_total(n):
+        full, rem = divmod(n, bi)
+        return r * full + (_live_slots(rem, threads, r) if rem else 0)
+    every = sum(p * r * -(-n // bi) for n, p in zip(sizes, npad))
+    live = cfg >= 0 and sum(p * live_total(n) for n, p in zip(sizes, npad)) < 0.99 * every
+    if len(sizes) == 300 or sizes == [100, 300, 70, 2000]:
+        assert live  # these cases exercise the weighted plan
     for c in range(g):
         for sys_, it, j0, j1, fix, part in segs[begin[c]:begin[c + 1]]:
             assert j0 < j1
@@ -221,12 +244,13 @@ def test_plan_work_covers_every_tile_once(sizes, cfg, grid):
                 key = (sys_, it, jt)
                 assert key not in covered
                 covered[key] = c
-                cost[c] += min(bj, npad[sys_] - jt * bj)
+                w = _live_slots(sizes[sys_] - it * bi, threads, r) if live else 1
+                cost[c] += min(bj, npad[sys_] - jt * bj) * w
     want = {(s, it, jt) for s, n in enumerate(sizes) for it in range((n + bi - 1) // bi)
             for jt in range((npad[s] + bj - 1) // bj)}
     assert set(covered) == want
-    # balance: every CTA within one j-tile of the mean charge
-    assert cost.max() - cost.min() <= 2 * bj
+    # balance: every CTA within one block of the mean charge
+    assert cost.max() - cost.min() <= 2 * bj * (r if live else 1)
     # fixups: parts of a split i-tile are numbered 0.. in j order
     parts = {}
     for sys_, it, j0, j1, fix, part in segs:
@@ -311,11 +335,11 @@ def test_null_handles_are_rejected_without_touching_the_device():
     assert "NULL" in L.nb_last_error().decode()
 
 
-@pytest.mark.parametrize("n,cfg,grid", [(1 << 20, 1, 152), (1 << 20, 1, 456), (262144, 0, 152),
-                                        (262144, 0, 456), (300000, 1, 152), (25600, 3, 50)])
+@pytest.mark.parametrize("n,cfg,grid", [(1 << 20, -1, 152), (262144, -1, 152), (300000, -1, 152),
+                                        (262144, -2, 456), (1 << 20, -2, 608), (25600, -3, 152)])
 def test_ordered_hand_over_schedule_never_waits(n, cfg, grid):
-    """The reference-order kernel's schedule, replayed on the work-list planner with
-    unit cost per j-tile: each CTA walks its segments last to first, and the part of
+    """The reference-order kernel's schedule, replayed on its own work list (shape
+    -1 - cfg, unit cost per j-tile): each CTA walks its segments last to first, and the part of
     a split i-tile may start only when the previous part has finished.  With at most
     one CTA per i-tile (the kernel's grid rule) no part waits and no i-tile is split
     into more than two parts."""
