@@ -937,7 +937,7 @@ int nb_kernel_config_info(int32_t index, nb_kernel_info* info) {
   if (!info || index < -reference_order_num_shapes() || index >= num_force_configs())
     return set_error(NB_ERR_INVALID_ARGUMENT, "bad config index");
   const KernelShape sh = index >= 0 ? force_config_shape(index) : reference_order_shape(-1 - index);
-  *info = nb_kernel_info{index, sh.threads, sh.r, sh.bj, sh.stages, 0, 0, 0};
+  *info = nb_kernel_info{index, sh.threads, sh.r, sh.bj, sh.stages, 0, 0, 0, 0};
   return NB_OK;
 }
 
@@ -968,12 +968,12 @@ int nb_sim_kernel_info(const nb_sim* s, nb_kernel_info* info) {
   if (sequential_order_mode(s)) {
     const KernelShape sh = reference_order_shape(s->ro_shape);
     *info = nb_kernel_info{-1 - s->ro_shape, sh.threads, sh.r, sh.bj, sh.stages,
-                           s->ro_wl.grid, s->ro_wl.nseg, s->ro_wl.split};
+                           s->ro_wl.grid, s->ro_wl.nseg, s->ro_wl.split, 0};
     return NB_OK;
   }
   const KernelShape sh = force_config_shape(s->cfg);
   *info = nb_kernel_info{s->cfg, sh.threads, sh.r, sh.bj, sh.stages,
-                         s->wl.grid, s->wl.nseg, s->wl.split};
+                         s->wl.grid, s->wl.nseg, s->wl.split, s->wl.live ? 1 : 0};
   return NB_OK;
 }
 

@@ -66,7 +66,7 @@ class nb_diagnostics(C.Structure):
 class nb_kernel_info(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("config_index", "threads_per_block",
                                           "particles_per_thread", "j_tile", "stages", "grid",
-                                          "segments", "split_tiles")]
+                                          "segments", "split_tiles", "live_slots")]
 
 
 class nb_segment(C.Structure):

@@ -107,6 +107,9 @@ typedef struct nb_kernel_info {
   int32_t grid;                 /* persistent CTAs per launch               */
   int32_t segments;             /* work-list entries                        */
   int32_t split_tiles;          /* i-tiles whose j-range spans several CTAs */
+  int32_t live_slots;           /* 1: the variant that skips the register slots
+                                   past the end of a system in its last i-tile,
+                                   with a work list weighted by live slots     */
 } nb_kernel_info;
 
 /* One entry of the persistent force kernel's work list: i-tile `i_tile` of
