@@ -119,6 +119,31 @@ def test_thin_disk_25600_accelerations_against_fp64():
         assert np.allclose(a, b[rows], rtol=1e-10, atol=1e-12)
 
 
+@pytest.mark.parametrize("acc", [nb.ACC_PLAIN, nb.ACC_COMPENSATED, nb.ACC_REFERENCE_ORDER])
+def test_two_body_known_answer(acc):
+    # Two unit masses a distance d apart along a direction u: each accelerates
+    # towards the other with G d / (d^2 + eps)^(3/2) (simulator.cu:200-206), equal
+    # and opposite to the last bit; one step from rest with damping 1 moves each by
+    # a dt^2 (:214-228).
+    d, eps, G, dt = 0.75, 1e-3, 2.0, 1e-2
+    u = np.array([2.0, -1.0, 2.0]) / 3.0
+    p0, p1 = -0.5 * d * u, 0.5 * d * u
+    pos = [np.array([p0[c], p1[c]], np.float32) for c in range(3)]
+    vel = [np.zeros(2, np.float32)] * 3
+    m = np.ones(2, np.float32)
+    with nb.Simulation(params(2, G=G, dt=dt, damping=1.0, eps=eps, acc=acc), pos, vel, m) as sim:
+        a = sim.accelerations()
+        sim.advance(1)
+        st = sim.get_state()
+    r = np.array([pos[c][1] - pos[c][0] for c in range(3)], np.float64)
+    want = G * r / (float(r @ r) + eps) ** 1.5
+    for c in range(3):
+        assert np.isclose(a[c][0], want[c], rtol=2e-6, atol=1e-7), (c, a[c][0], want[c])
+        assert a[c][1] == -a[c][0]
+        assert np.isclose(st[3 + c][0], want[c] * dt, rtol=2e-6, atol=1e-9)
+        assert np.isclose(st[c][0], pos[c][0] + want[c] * dt * dt, rtol=1e-6, atol=1e-9)
+
+
 def test_zero_softening_excludes_self_pair():
     # eps = 0: the self term would be 0 * inf; the reference skips it (:206).
     n = 700
