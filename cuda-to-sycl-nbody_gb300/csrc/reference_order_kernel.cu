@@ -396,19 +396,29 @@ struct RoShapeEntry {
 #define RO_SHAPE(T, P, BJ, U, B)                                                   \
   {T, P, BJ, {reference_order_kernel<T, P, BJ, U, B, false>,                       \
               reference_order_kernel<T, P, BJ, U, B, true>}}
-// Largest i-tiles first.  Measured at N = 1M (fraction of nominal FP32 peak, one
-// launch): 384 x 2 with 1024-particle j-tiles 69.8 % (12 warps, one CTA per SM);
-// 384 x 2 x 256 69.0 %; 512 x 2 67.9 % (16 warps, 128 registers); 256 x 2 66.5 %
-// (8 warps); 128 x 4 65.9 %; 128 x 2 64.2 %; 448 x 2 and 320 x 2 (warps not a
-// multiple of the SM's four schedulers) 59 %; 64 x 1 53.4 %; 384 x 2 x 2048 69.9 %,
-// 256 x 4 69.4 %, 384 x 3 69.2 %, 256 x 3 68.3 %, 384 x 2 with 2 j steps per unrolled
-// block 65.5 % (at N = 262,144 the three-and-four-pair shapes fall to 51-68 %: fewer,
-// larger i-tiles balance worse).  The small shapes
-// serve systems too small to fill the GPU with the large i-tiles.
+// Largest i-tiles first; the default for a system is the first shape whose i-tiles
+// give every SM two CTAs (one where only one fits), else the last.  Measured
+// (thin disk, ms per step; every variant gave the same bits):
+//   * N = 1M and 262,144: 384 x 2 x 1024 (12 warps, one CTA per SM, 4 j-steps per
+//     unrolled block) 390.9 / 24.6 ms, 69.8 % of nominal FP32 peak at 1M.  Deeper
+//     unrolling (16 j-steps) 398.0 / 25.0; 128 x 2, 256 x 1 and 64 x 1 shapes
+//     418-445 / 25.3-27.8; 512 x 2 67.9 % and 256 x 2 66.5 % at 1M; 448 x 2 and
+//     320 x 2 (warps not a multiple of the SM's four schedulers) 59 %; 256 x 4,
+//     384 x 3 and 256 x 3 68.3-69.4 % at 1M but 51-68 % at 262,144.
+//   * Below that, few i-tiles leave each scheduler about one warp, and what hides the
+//     pair chain's latency (about 80 cycles from shared load to accumulate) is the
+//     number of independent j-steps a thread has in flight: one i-pair per thread,
+//     32 j-steps per unrolled block (128 registers).  At 196,608: 256 x 1 x 1024
+//     14.2 ms (384 x 2 16.4, 128 x 2 x 256 with 4 j-steps 17.7); at 131,072:
+//     128 x 1 x 1024 6.61 (64 x 1 x 1024 6.98, 384 x 2 10.9); at 65,536:
+//     64 x 1 x 1024 1.76 (128 x 2 x 256 2.25); at 25,600: 0.418 (64 x 1 x 256 with
+//     4 j-steps 0.605); at 2,048: 0.045 (0.057).  2048-particle j-tiles (one CTA
+//     per SM) halve the rate of the 64-thread shape.
 const RoShapeEntry kRoShapes[] = {
     RO_SHAPE(384, 2, 1024, 4, 1),
-    RO_SHAPE(128, 2, 256, 4, 1),
-    RO_SHAPE(64, 1, 256, 4, 1),
+    RO_SHAPE(256, 1, 1024, 32, 1),
+    RO_SHAPE(128, 1, 1024, 32, 1),
+    RO_SHAPE(64, 1, 1024, 32, 1),
 };
 constexpr int kNumRoShapes = sizeof(kRoShapes) / sizeof(kRoShapes[0]);
 

@@ -336,7 +336,8 @@ def test_null_handles_are_rejected_without_touching_the_device():
 
 
 @pytest.mark.parametrize("n,cfg,grid", [(1 << 20, -1, 152), (262144, -1, 152), (300000, -1, 152),
-                                        (262144, -2, 456), (1 << 20, -2, 608), (25600, -3, 152)])
+                                        (262144, -2, 456), (1 << 20, -2, 608), (200000, -2, 304),
+                                        (150000, -3, 304), (25600, -4, 152), (65536, -4, 304)])
 def test_ordered_hand_over_schedule_never_waits(n, cfg, grid):
     """The reference-order kernel's schedule, replayed on its own work list (shape
     -1 - cfg, unit cost per j-tile): each CTA walks its segments last to first, and the part of

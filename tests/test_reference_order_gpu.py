@@ -211,7 +211,7 @@ def test_thousand_steps_bitwise_equal_to_reference_kernel():
 
 
 @needs_reference
-@pytest.mark.parametrize("n", [25600, 300000, 1 << 20])
+@pytest.mark.parametrize("n", [25600, 150000, 200000, 300000, 1 << 20])
 def test_every_shape_and_autotune_stay_bitwise(n):
     """The default shape depends on the size: the largest i-tiles that still fill the
     GPU (the stream-K grid hands split i-tiles over between CTAs); the autotuner
@@ -227,11 +227,11 @@ def test_every_shape_and_autotune_stay_bitwise(n):
         assert chosen <= -1 and sim.kernel_info()["config_index"] == chosen
         sim.advance(2)
         got = sim.get_state()
-    assert default <= -1
-    if n == 25600:
-        assert default == -3          # 64 x 1: 200 i-tiles (384 x 2 would give 17)
-    else:
-        assert default == -1          # 384 x 2: 196 (n = 300,000) or 683 i-tiles
+    # the largest i-tiles that give every SM two CTAs (one for 384 x 2, where only one
+    # fits): 384 x 2 (1536 particles) from 233,472 up; 256 x 1 (512) from 155,648;
+    # 128 x 1 (256) from 77,824; below that 64 x 1 (128)
+    want = {25600: -4, 150000: -3, 200000: -2, 300000: -1, 1 << 20: -1}[n]
+    assert default == want, (n, default)
     assert same_bits(got, ref)
 
 
@@ -258,6 +258,6 @@ def test_shape_selection_by_index_stays_bitwise():
             sim.advance(2)
             assert same_bits(sim.get_state(), ref), shapes
             shapes += 1
-        assert shapes == 3
+        assert shapes == 4
         sim.set_kernel_config(-1)                     # back to the default
         assert sim.kernel_info()["config_index"] <= -1
