@@ -174,27 +174,31 @@ __global__ void __launch_bounds__(kAdjThreads) adjoint_partial_kernel(const Adjo
 }
 
 // lx = lx' + dt * gscale * sum over chunks (in chunk order) and lv = damping * mu,
-// real particles only.
-__global__ void adjoint_combine_kernel(const AdjointArgs a) {
+// real particles only.  One thread per particle, kCombineThreads particles of an
+// i-tile per CTA (blockIdx.y picks them); the chunk loop is unrolled so that several
+// of its loads are in flight (the additions keep their order).
+constexpr int kCombineThreads = 128;
+static_assert(kAdjBI % kCombineThreads == 0, "whole i-tiles");
+
+__global__ void __launch_bounds__(kCombineThreads) adjoint_combine_kernel(const AdjointArgs a) {
   const SystemDesc sd = a.sys[a.tile_sys[blockIdx.x]];
   const int ibase = a.tile_idx[blockIdx.x] * kAdjBI;
   const float c = a.dt * sd.gscale;
-  for (int k = threadIdx.x; k < kAdjBI; k += blockDim.x) {
-    const int li = ibase + k;
-    if (li >= sd.n) break;
-    const int64_t g = sd.offset + li;
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    for (int s = 0; s < a.num_splits; ++s) {
-      const float4 p = a.partial[static_cast<int64_t>(s) * a.n_pad + g];
-      sx += p.x;
-      sy += p.y;
-      sz += p.z;
-    }
-    const float4 l = a.lam_x[g], v = a.lam_v[g];
-    a.lam_x_out[g] = make_float4(fmaf(c, sx, l.x), fmaf(c, sy, l.y), fmaf(c, sz, l.z), 0.f);
-    a.lam_v_out[g] = make_float4(a.damping * fmaf(a.dt, l.x, v.x), a.damping * fmaf(a.dt, l.y, v.y),
-                                 a.damping * fmaf(a.dt, l.z, v.z), 0.f);
+  const int li = ibase + blockIdx.y * kCombineThreads + threadIdx.x;
+  if (li >= sd.n) return;
+  const int64_t g = sd.offset + li;
+  float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll 8
+  for (int s = 0; s < a.num_splits; ++s) {
+    const float4 p = a.partial[static_cast<int64_t>(s) * a.n_pad + g];
+    sx += p.x;
+    sy += p.y;
+    sz += p.z;
   }
+  const float4 l = a.lam_x[g], v = a.lam_v[g];
+  a.lam_x_out[g] = make_float4(fmaf(c, sx, l.x), fmaf(c, sy, l.y), fmaf(c, sz, l.z), 0.f);
+  a.lam_v_out[g] = make_float4(a.damping * fmaf(a.dt, l.x, v.x), a.damping * fmaf(a.dt, l.y, v.y),
+                               a.damping * fmaf(a.dt, l.z, v.z), 0.f);
 }
 
 __global__ void unpack_vec3_kernel(const float* __restrict__ in, int64_t n,
@@ -244,7 +248,8 @@ cudaError_t launch_adjoint(const AdjointArgs& a, int32_t num_tiles, bool per_pai
     adjoint_partial_kernel<false><<<grid, kAdjThreads, 0, stream>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  adjoint_combine_kernel<<<num_tiles, 256, 0, stream>>>(a);
+  adjoint_combine_kernel<<<dim3(num_tiles, kAdjBI / kCombineThreads), kCombineThreads, 0,
+                           stream>>>(a);
   return cudaGetLastError();
 }
 
